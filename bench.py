@@ -1,0 +1,406 @@
+#!/usr/bin/env python
+"""Benchmark of the TracerAdvectionDiffusion time step on GB300.
+
+Workload (the 2D cellular-flow configuration the headline metric is quoted
+on): ψ = U cos(kx) cos(ky) with k = 4, U = 1 (u = -∂ψ/∂y, v = ∂ψ/∂x), Lx = Ly =
+2π, nx = ny = 1024, κ = η = 1e-4, hyperdiffusion κh = 1e-12 on ∇⁴ (nκh = 2),
+ETDRK4.  Initial conditions are Gaussians of σ = 0.2 at seeded random centres
+(synthetic data).
+
+* ``value``: the FP32-batched form -- ``--batch`` independent solves (an
+  ensemble of initial conditions) stepped together, FP32 bulk transforms with
+  FP64 ETDRK4 coefficients.  Unit: grid-point-steps/s = batch·nx·ny·steps/s.
+  The batch state (≈30 MB per solve) is larger than L2, so consecutive steps
+  are timed back to back.
+* ``fp64_plain``: one FP64 solve of the same workload (the drop-in path),
+  each timed step preceded by an L2 flush.
+* ``dt`` defaults to 5e-4: the workload's nominal dt = 2e-3 gives an advective
+  CFL number u_max·k_max·dt = 4·512·2e-3 ≈ 4.1 at 1024², beyond the
+  ETDRK4/RK4 stability limit (≈2.8); the FP64 CPU oracle itself diverges after
+  ≈22 steps there.  The cost of a step does not depend on dt.
+
+``--impl reference`` times the CPU FP64 oracle restatement of the reference
+(NumPy + pocketfft on all host cores): the reference's own Julia code cannot
+run on these machines (no Julia).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "grid-pt-steps/s (FP32-batched, rel-L2<=1e-5 vs FP64 oracle; FP64 plain beside)"
+UNIT = "grid-pt-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1024)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--dt", type=float, default=5e-4)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-oracle-check", action="store_true")
+    return ap.parse_args()
+
+
+def workload(args, batch):
+    return {
+        "workload": f"2D cellular flow {args.n}x{args.n}, ETDRK4, psi=U cos(4x)cos(4y) U=1, kappa=eta=1e-4, "
+                    f"kappah=1e-12 nkappah=2, dt={args.dt:g}",
+        "nx": args.n, "ny": args.n, "stepper": "ETDRK4", "dt": args.dt, "nominal_dt": 0.002,
+        "batch_per_gpu": batch, "precision": "FP32 bulk, FP64 ETDRK4 coefficients",
+        "l2_policy": "batch state larger than L2 (FP32 batched); L2 flushed before every timed step (FP64 plain)",
+    }
+
+
+def flow_fns():
+    u = lambda x, y: 4.0 * np.cos(4 * x) * np.sin(4 * y)
+    v = lambda x, y: -4.0 * np.sin(4 * x) * np.cos(4 * y)
+    return u, v
+
+
+def initial_conditions(n, batch, seed):
+    rng = np.random.default_rng(seed)
+    x = -np.pi + 2 * np.pi / n * np.arange(n)
+    Y, X = np.meshgrid(x, x, indexing="ij")
+    out = np.empty((batch, n, n))
+    for b in range(batch):
+        x0, y0 = rng.uniform(-np.pi, np.pi, 2) if b else (np.pi / 2, np.pi / 2)
+        dx = (X - x0 + np.pi) % (2 * np.pi) - np.pi
+        dy = (Y - y0 + np.pi) % (2 * np.pi) - np.pi
+        out[b] = np.exp(-(dx ** 2 + dy ** 2) / (2 * 0.2 ** 2))
+    return out
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = [ln.split(",") for ln in Path(self.path).read_text().splitlines() if ln.strip()]
+        os.unlink(self.path)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1])); smax = float(r[2])
+                for nm, val in zip(names, r[5:9]):
+                    if val.strip() == "Active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def oracle_module():
+    import __graft_entry__ as g
+    return g._load_module_file("ptf_oracle", ROOT / "oracle" / "ptf_oracle.py")
+
+
+def oracle_problem(o, n, dt):
+    u, v = flow_fns()
+    return o.Problem(o.TwoDAdvectingFlow(u=u, v=v), nx=n, Lx=2 * np.pi, kappa=1e-4, eta=1e-4, kappah=1e-12,
+                     nkappah=2, dt=dt, stepper="ETDRK4")
+
+
+def cpu_oracle_rate(args, seconds, max_steps):
+    """Time the FP64 oracle (all host cores) on a bounded sample of the workload."""
+    o = oracle_module()
+    p = oracle_problem(o, args.n, args.dt)
+    o.set_c(p, initial_conditions(args.n, 1, 0)[0])
+    o.stepforward(p, 1)  # warm-up (plans, caches)
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < max_steps and (time.perf_counter() - t0) < seconds:
+        o.stepforward(p, 1)
+        steps += 1
+    el = time.perf_counter() - t0
+    return args.n * args.n * steps / el, steps, el, o.WORKERS
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    K = max(1, min(args.steps, 40))
+    W = max(0, min(args.warmup, 3))
+    o = oracle_module()
+    p = oracle_problem(o, args.n, args.dt)
+    o.set_c(p, initial_conditions(args.n, 1, 0)[0])
+    o.stepforward(p, W)
+    t0 = time.perf_counter()
+    o.stepforward(p, K)
+    el = time.perf_counter() - t0
+    val = args.n * args.n * K / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": K,
+        "warmup": W, "ms_per_step": 1e3 * el / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": dict(workload(args, 1), precision="FP64 (CPU oracle)"),
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": o.WORKERS, "kind": "port",
+                         "sample": f"{K} ETDRK4 steps of one {args.n}x{args.n} solve after {W} warm-up steps "
+                                   "(NumPy/pocketfft FP64 restatement; Julia is not available)"},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    import __graft_entry__ as g
+    lib_path = g.PKG_DIR / "libptf.so"
+    if not lib_path.exists():
+        g.build()
+    pkg = g.load_package()
+    from ptf_gb300 import _lib as L
+    lib = L.load()
+    n, B, K, W, dt = args.n, args.batch, args.steps, max(3, args.warmup), args.dt
+    u, v = flow_fns()
+    kw = dict(nx=n, Lx=2 * np.pi, κ=1e-4, η=1e-4, κh=1e-12, nκh=2, dt=dt, stepper="ETDRK4")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    c0 = initial_conditions(n, B, 1234 + rank)
+    # ---------------- FP32 batched ----------------
+    p32 = pkg.Problem(pkg.GPU(), pkg.TwoDAdvectingFlow(u=u, v=v), T=np.float32, batch=B, **kw)
+    pkg.set_c(p32, c0)
+    st32 = torch.cuda.ExternalStream(p32.stream)
+    pkg.stepforward(p32, W)
+    sampler = ClockSampler(torch.cuda.current_device())
+    sampler.start()
+    time.sleep(0.3)
+    barrier()
+    launches0 = p32.kernel_launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st32)
+    pkg.stepforward(p32, K)
+    e1.record(st32)
+    e1.synchronize()
+    barrier()
+    ms32 = max_over_ranks(e0.elapsed_time(e1))
+    launches = p32.kernel_launches - launches0
+    value = world * B * n * n * K / (ms32 / 1e3)
+    # per-pass roofline (same stream, CUDA events around each pass)
+    lib.ptf_profile(p32._h, 1)
+    pkg.stepforward(p32, K)
+    prof = {}
+    for kind, name in ((0, "column_pass"), (1, "row_pass")):
+        ms, cnt, by = ct_read(lib, p32._h, kind)
+        prof[name] = {"ms": ms, "launches": cnt, "bytes": by}
+    lib.ptf_profile(p32._h, 0)
+    steps32 = W + 2 * K
+    # ---------------- FP64 plain ----------------
+    p64 = pkg.Problem(pkg.GPU(), pkg.TwoDAdvectingFlow(u=u, v=v), T=np.float64, batch=1, **kw)
+    pkg.set_c(p64, c0[0])
+    st64 = torch.cuda.ExternalStream(p64.stream)
+    pkg.stepforward(p64, W)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    K64 = K
+    barrier()
+    evs = []
+    with torch.cuda.stream(st64):
+        for _ in range(K64):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st64)
+            pkg.stepforward(p64, 1)
+            b.record(st64)
+            evs.append((a, b))
+    torch.cuda.synchronize()
+    ms64 = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs))
+    value64 = world * n * n * K64 / (ms64 / 1e3)
+    lib.ptf_profile(p64._h, 1)
+    pkg.stepforward(p64, 8)
+    prof64 = {}
+    for kind, name in ((0, "column_pass"), (1, "row_pass")):
+        ms, cnt, by = ct_read(lib, p64._h, kind)
+        prof64[name] = {"ms": ms, "launches": cnt, "bytes": by}
+    lib.ptf_profile(p64._h, 0)
+    steps64 = W + K64 + 8
+    clocks = sampler.stop()
+    # ---------------- accuracy vs the FP64 oracle ----------------
+    acc = {}
+    pkg.updatevars(p32)
+    pkg.updatevars(p64)
+    c32 = p32.vars.c[0].copy()
+    c64 = p64.vars.c.copy()
+    if rank == 0 and not args.no_oracle_check:
+        o = oracle_module()
+        # continue the FP64 GPU solve to the FP32 solve's step count, then compare both with the oracle
+        pkg.stepforward(p64, steps32 - steps64)
+        pkg.updatevars(p64)
+        c64 = p64.vars.c.copy()
+        po = oracle_problem(o, n, dt)
+        o.set_c(po, c0[0])
+        t0 = time.perf_counter()
+        o.stepforward(po, steps32)
+        o.updatevars(po)
+        m0 = float(c0[0].sum())
+        acc = {
+            "steps": steps32,
+            "rel_l2_fp32_vs_oracle": o.rel_l2(c32, po.vars.c),
+            "rel_l2_fp64_vs_oracle": o.rel_l2(c64, po.vars.c),
+            "mass_drift_fp32": float(c32.sum()) / m0 - 1,
+            "mass_drift_fp64": float(c64.sum()) / m0 - 1,
+            "mass_drift_oracle": float(po.vars.c.sum()) / m0 - 1,
+            "oracle_seconds": time.perf_counter() - t0,
+        }
+    # ---------------- end to end through the public API ----------------
+    S = min(25, K)
+    frames = max(1, K // S)
+    pin_in = torch.empty((B, n, n), dtype=torch.float64, pin_memory=True)
+    pin_in.numpy()[...] = c0
+    pin_out = torch.empty((B, n, n), dtype=torch.float64, pin_memory=True)
+    p32.vars.c = pin_out.numpy()
+    barrier()
+    t0 = time.perf_counter()
+    pkg.set_c(p32, pin_in.numpy())
+    for _ in range(frames):
+        pkg.stepforward(p32, S)
+        pkg.updatevars(p32)
+    t1 = time.perf_counter()
+    e2e_s = max_over_ranks(t1 - t0)
+    e2e_val = world * B * n * n * frames * S / e2e_s
+    bytes_field = B * n * n * 8
+    # ---------------- CPU baseline (rank 0) ----------------
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        rate, steps, el, cores = cpu_oracle_rate(args, args.cpu_seconds, 200)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{steps} ETDRK4 steps of one {n}x{n} FP64 solve ({el:.1f} s, NumPy/pocketfft restatement)"}
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    hbm_peak, peak_kind = load_peaks()
+    dom = max(prof, key=lambda k: prof[k]["ms"])
+    d = prof[dom]
+    achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9
+    roof = {"bound": "hbm", "kernel": f"{dom} (FP32, {n}x{n}, batch {B})", "achieved": achieved, "peak": hbm_peak,
+            "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm_peak,
+            "traffic": None, "avg_launch_us": 1e3 * d["ms"] / max(1, d["launches"]),
+            "algorithmic_bytes_per_launch": d["bytes"] / max(1, d["launches"]),
+            "share_of_step": d["ms"] / sum(x["ms"] for x in prof.values())}
+    passes = {k: {"ms_per_launch": x["ms"] / max(1, x["launches"]), "GBps": x["bytes"] / (x["ms"] / 1e3) / 1e9,
+                  "launches": x["launches"]} for k, x in prof.items()}
+    passes64 = {k: {"ms_per_launch": x["ms"] / max(1, x["launches"]), "GBps": x["bytes"] / (x["ms"] / 1e3) / 1e9,
+                    "launches": x["launches"]} for k, x in prof64.items()}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms32 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded Gaussian ensemble on the cellular flow)",
+        "config": dict(workload(args, B), parallelism="replicas" if world > 1 else "single GPU"),
+        "fp64_plain": {"value": value64, "unit": UNIT, "ms_per_step": ms64 / K64, "steps": K64, "dtype": "f64",
+                       "passes": passes64, "ratio_fp32_batched_over_fp64": value / value64},
+        "accuracy": acc,
+        "passes": passes,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": bytes_field / (frames * S),
+                "d2h_bytes_per_step": bytes_field / S,
+                "api": f"set_c(pinned host) + {frames} x (stepforward({S}) + updatevars(pinned host))"},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def ct_read(lib, h, kind):
+    import ctypes as ct
+    ms, cnt, by = ct.c_double(), ct.c_int64(), ct.c_double()
+    rc = lib.ptf_profile_read(h, kind, ct.byref(ms), ct.byref(cnt), ct.byref(by))
+    if rc:
+        raise RuntimeError(f"ptf_profile_read failed ({rc})")
+    return ms.value, cnt.value, by.value
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

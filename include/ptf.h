@@ -1,0 +1,133 @@
+/*
+ * ptf.h -- C ABI of libptf.so, the GB300 (sm_103a) implementation of the
+ * PassiveTracerFlows.jl TracerAdvectionDiffusion time step.
+ *
+ * Every entry point replaces one piece of the reference's path; the
+ * reference location is cited beside each declaration (paths are relative
+ * to the PassiveTracerFlows.jl repository).  FourierFlows.jl 0.10.5 is the
+ * framework the reference plugs into (Project.toml:23); its functions are
+ * named where the reference calls them.
+ *
+ * Conventions
+ *  - Every function returns 0 on success or a positive PTF_ERR_* code; it
+ *    never aborts.  ptf_last_error() gives the message of the last failure
+ *    on a handle (or of the last ptf_create failure for NULL).
+ *  - The handle owns all of its device memory and one CUDA stream.  A handle
+ *    is not thread-safe; distinct handles are independent.
+ *  - Array arguments are FP64 in the reference's column-major layout (x
+ *    fastest): physical fields are nx*ny[*nz] doubles, spectral fields are
+ *    (nx/2+1)*ny[*nz] complex doubles stored (re, im) interleaved.  With
+ *    batch > 1 the solves follow one another.  `where` says whether a
+ *    pointer is host (PTF_HOST) or device (PTF_DEVICE) memory.
+ *  - Calls taking a host pointer return after the copy is complete; calls on
+ *    device pointers and ptf_step are ordered on the handle's stream and may
+ *    return before the GPU is done (ptf_synchronize waits).
+ */
+#ifndef PTF_H
+#define PTF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PTF_ABI_VERSION 1
+
+enum ptf_status {
+  PTF_OK = 0,
+  PTF_ERR_ARG = 1,         /* invalid argument (reference: ArgumentError) */
+  PTF_ERR_CUDA = 2,        /* CUDA runtime error */
+  PTF_ERR_STATE = 3,       /* call out of order (e.g. step before set_c) */
+  PTF_ERR_UNSUPPORTED = 4, /* valid for the reference, not built here */
+  PTF_ERR_MEMORY = 5       /* device memory budget exceeded */
+};
+
+enum ptf_stepper { PTF_RK4 = 0, PTF_ETDRK4 = 1 };
+enum ptf_precision { PTF_FP64 = 0, PTF_FP32 = 1 };
+/* PTF_CLOCK_T evaluates a time-varying flow at clock.t for all four stages
+ * of a step, as the reference does (src/traceradvectiondiffusion.jl:718,737);
+ * PTF_STAGE_T evaluates it at each stage time (an extension). */
+enum ptf_time_mode { PTF_CLOCK_T = 0, PTF_STAGE_T = 1 };
+enum ptf_where { PTF_HOST = 0, PTF_DEVICE = 1 };
+
+/* Mirrors the keyword arguments of TracerAdvectionDiffusion.Problem
+ * (src/traceradvectiondiffusion.jl:165-216).  kappah / nkappah are the
+ * hyperdiffusion of ConstDiffSteadyFlowParams (:436-452), which the
+ * reference reaches only through its low-level constructor. */
+typedef struct ptf_config {
+  int32_t dim;        /* 2 or 3 */
+  int32_t nx, ny, nz; /* powers of two, 16..4096 (nz ignored for dim 2) */
+  double Lx, Ly, Lz;
+  double kappa, eta, iota; /* x, y, z diffusivities */
+  double kappah;           /* hyperdiffusivity */
+  int32_t nkappah;         /* hyperdiffusivity order (0: none) */
+  double dt;
+  int32_t stepper;   /* ptf_stepper */
+  int32_t precision; /* ptf_precision */
+  int32_t time_mode; /* ptf_time_mode */
+  int32_t batch;     /* independent solves sharing grid, parameters and flow */
+} ptf_config;
+
+typedef struct ptf_handle ptf_handle;
+
+/* Fill a config with the reference's defaults: nx=ny=nz=128, L=2pi,
+ * kappa=0.1, eta=iota=kappa, dt=0.01, RK4, FP64, batch 1. */
+void ptf_config_default(ptf_config* cfg, int32_t dim);
+
+/* TracerAdvectionDiffusion.Problem(dev, flow; ...) construction:
+ * grid (:177,:205), Equation L (:538-554), Vars (:652-668) and the
+ * FourierFlows time stepper state (FourierFlows.Problem, :187,:215). */
+int ptf_create(const ptf_config* cfg, ptf_handle** out);
+void ptf_destroy(ptf_handle* h);
+const char* ptf_last_error(const ptf_handle* h);
+
+/* Steady flow arrays u.(x,y[,z]), v, w on the grid: the precomputation of
+ * ConstDiffSteadyFlowParams (:436-452).  Also used for a time-varying flow
+ * re-evaluated by the caller at clock.t before each step (:715-718). */
+int ptf_set_flow_arrays(ptf_handle* h, const double* u, const double* v, const double* w, int32_t where);
+
+/* set_c!(prob, c) (:844-852, :872): sol = rfft(c). */
+int ptf_set_c(ptf_handle* h, const double* c, int32_t where);
+/* updatevars!(prob) then copy vars.c out (:815-821, :837). */
+int ptf_get_c(ptf_handle* h, double* c, int32_t where);
+/* prob.sol out / in (complex, (nx/2+1)*ny[*nz] per solve). */
+int ptf_get_sol(ptf_handle* h, double* sol, int32_t where);
+int ptf_set_sol(ptf_handle* h, const double* sol, int32_t where);
+
+/* stepforward!(prob, nsteps) (FourierFlows; called at
+ * test/test_traceradvectiondiffusion.jl:29): nsteps RK4/ETDRK4 steps, each
+ * followed by clock.t += dt, clock.step += 1. */
+int ptf_step(ptf_handle* h, int64_t nsteps);
+/* prob.clock.t, prob.clock.step */
+int ptf_clock(const ptf_handle* h, double* t, int64_t* step);
+int ptf_set_clock(ptf_handle* h, double t, int64_t step);
+
+/* calcN!(N, sol, t, clock, vars, params, grid) (:756-769 / :771-786): the
+ * FourierFlows Equation plugin on its own: N = rfft(-(u.grad c)) for the
+ * spectral field `sol`, with the flow set on the handle.  Complex arrays. */
+int ptf_calcN(ptf_handle* h, const double* sol, double* N, int32_t where);
+
+int ptf_synchronize(ptf_handle* h);
+/* The handle's CUDA stream (cudaStream_t) and an override of it. */
+int ptf_get_stream(const ptf_handle* h, void** stream);
+int ptf_set_stream(ptf_handle* h, void* stream);
+/* Bytes of device memory held by the handle. */
+int ptf_device_bytes(const ptf_handle* h, int64_t* bytes);
+/* Per-pass timing: with enable != 0 every pass launch is bracketed by CUDA
+ * events on the handle's stream (enabling or disabling clears the record).
+ * ptf_profile_read sums, for kind 0 (column passes: y transforms + stepper
+ * stage) or 1 (row passes: x transforms + advection product), the event
+ * time in ms, the launch count and the algorithmic bytes of those launches
+ * (the minimum HBM traffic of the pass design).  No reference counterpart:
+ * the reference has no profiling hooks. */
+int ptf_profile(ptf_handle* h, int32_t enable);
+int ptf_profile_read(ptf_handle* h, int32_t kind, double* total_ms, int64_t* launches, double* bytes);
+/* Kernels launched by this handle since creation (for launch accounting). */
+int ptf_kernel_launches(const ptf_handle* h, int64_t* count);
+int32_t ptf_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PTF_H */

@@ -1,0 +1,20 @@
+"""GB300-native TracerAdvectionDiffusion time step with the PassiveTracerFlows.jl API.
+
+``import`` name: the directory is ``passivetracerflows.jl_gb300`` (mirroring the
+Julia package name), so it is loaded under the module name ``ptf_gb300`` by
+:func:`__graft_entry__.load_package` (or any ``importlib`` spec loader).
+
+Everything numerical runs in ``libptf.so`` (hand-written sm_103a CUDA, C ABI in
+``include/ptf.h``); this package holds the host-side mirror of the reference's
+user API, as PassiveTracerFlows.jl re-exports ``TracerAdvectionDiffusion``
+(``src/PassiveTracerFlows.jl:1-13``).
+"""
+from . import traceradvectiondiffusion as TracerAdvectionDiffusion
+from .traceradvectiondiffusion import (CPU, GPU, Problem, OneDAdvectingFlow, ThreeDAdvectingFlow,
+                                       TwoDAdvectingFlow, ThreeDGrid, TwoDGrid, gridpoints, noflow, set_c,
+                                       stepforward, updatevars)
+from ._lib import LIB_PATH, load as load_library
+
+__all__ = ["TracerAdvectionDiffusion", "CPU", "GPU", "Problem", "OneDAdvectingFlow", "TwoDAdvectingFlow",
+           "ThreeDAdvectingFlow", "TwoDGrid", "ThreeDGrid", "gridpoints", "noflow", "set_c", "stepforward",
+           "updatevars", "LIB_PATH", "load_library"]

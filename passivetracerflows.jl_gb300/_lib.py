@@ -1,0 +1,102 @@
+"""ctypes binding of libptf.so (the C ABI declared in include/ptf.h).
+
+The library is loaded from this package directory.  There is no fallback:
+if the library is missing or no CUDA device is present, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libptf.so"
+
+PTF_OK, PTF_ERR_ARG, PTF_ERR_CUDA, PTF_ERR_STATE, PTF_ERR_UNSUPPORTED, PTF_ERR_MEMORY = 0, 1, 2, 3, 4, 5
+PTF_RK4, PTF_ETDRK4 = 0, 1
+PTF_FP64, PTF_FP32 = 0, 1
+PTF_CLOCK_T, PTF_STAGE_T = 0, 1
+PTF_HOST, PTF_DEVICE = 0, 1
+
+
+class PtfConfig(ct.Structure):
+    _fields_ = [
+        ("dim", ct.c_int32), ("nx", ct.c_int32), ("ny", ct.c_int32), ("nz", ct.c_int32),
+        ("Lx", ct.c_double), ("Ly", ct.c_double), ("Lz", ct.c_double),
+        ("kappa", ct.c_double), ("eta", ct.c_double), ("iota", ct.c_double),
+        ("kappah", ct.c_double), ("nkappah", ct.c_int32),
+        ("dt", ct.c_double),
+        ("stepper", ct.c_int32), ("precision", ct.c_int32), ("time_mode", ct.c_int32),
+        ("batch", ct.c_int32),
+    ]
+
+
+class PtfError(RuntimeError):
+    """A libptf call returned a non-zero status."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"libptf error {code}: {msg}")
+        self.code = code
+
+
+class PtfArgumentError(PtfError, ValueError):
+    pass
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "ptf_abi_version": (ct.c_int32, []),
+    "ptf_config_default": (None, [ct.POINTER(PtfConfig), ct.c_int32]),
+    "ptf_create": (ct.c_int, [ct.POINTER(PtfConfig), ct.POINTER(ct.c_void_p)]),
+    "ptf_destroy": (None, [ct.c_void_p]),
+    "ptf_last_error": (ct.c_char_p, [ct.c_void_p]),
+    "ptf_set_flow_arrays": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int32]),
+    "ptf_set_c": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int32]),
+    "ptf_get_c": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int32]),
+    "ptf_get_sol": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int32]),
+    "ptf_set_sol": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int32]),
+    "ptf_step": (ct.c_int, [ct.c_void_p, ct.c_int64]),
+    "ptf_clock": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_double), ct.POINTER(ct.c_int64)]),
+    "ptf_set_clock": (ct.c_int, [ct.c_void_p, ct.c_double, ct.c_int64]),
+    "ptf_calcN": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int32]),
+    "ptf_synchronize": (ct.c_int, [ct.c_void_p]),
+    "ptf_get_stream": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_void_p)]),
+    "ptf_set_stream": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
+    "ptf_device_bytes": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_int64)]),
+    "ptf_kernel_launches": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_int64)]),
+    "ptf_profile": (ct.c_int, [ct.c_void_p, ct.c_int32]),
+    "ptf_profile_read": (ct.c_int, [ct.c_void_p, ct.c_int32, ct.POINTER(ct.c_double), ct.POINTER(ct.c_int64),
+                                    ct.POINTER(ct.c_double)]),
+}
+
+_lib = None
+
+
+def load(path: os.PathLike | None = None):
+    """Load libptf.so (once) and declare the C signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it first (passivetracerflows.jl_gb300/build.py)")
+    lib = ct.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc: int, handle=None):
+    if rc == PTF_OK:
+        return
+    msg = load().ptf_last_error(handle)
+    msg = msg.decode() if msg else ""
+    if rc == PTF_ERR_ARG:
+        raise PtfArgumentError(rc, msg)
+    if rc == PTF_ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    if rc == PTF_ERR_MEMORY:
+        raise MemoryError(msg)
+    raise PtfError(rc, msg)

@@ -1,0 +1,243 @@
+// Shared-memory Stockham FFT building blocks for sm_103a.
+//
+// A "line" of N complex values (N a power of two, 16 <= N <= 4096) is
+// transformed by N/E threads that each hold E = 16 values in registers.
+// Stages are radix-16 except one radix-2/4/8 stage when N is not a power
+// of 16.  Between stages the line is exchanged through shared memory
+// (padded index i + i/16 so that the stride-16 write pattern of the first
+// stage is bank-conflict free).  The algorithm is the Stockham autosort
+// decimation-in-time formulation (Govindaraju et al., SC'08): stage with
+// radix R after sub-transforms of size NS reads x[j + r*N/R], multiplies by
+// w_{NS*R}^{r*(j mod NS)}, does a radix-R DFT and writes
+// y[(j/NS)*NS*R + (j mod NS) + r*NS].  Output is in natural order.
+//
+// Register convention: thread t owns butterflies j = t + q*(N/E),
+// q = 0..E/R-1, and register v[q*R + r] holds element j + r*(N/R) at the
+// first-stage input and at the last-stage output (R = that stage's radix).
+// An inverse transform whose last radix equals the next forward
+// transform's first radix can therefore feed it with no shared-memory
+// exchange; the row pass relies on this.
+//
+// Twiddles come from a per-N table tw[m] = exp(-2*pi*i*m/N) computed on the
+// host in FP64 (octant symmetry on host libm values) and read through the
+// read-only cache; the inverse uses the conjugate.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ptf {
+
+template <typename T> struct cplx_of;
+template <> struct cplx_of<double> { typedef double2 type; };
+template <> struct cplx_of<float> { typedef float2 type; };
+
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C, typename T> __device__ __forceinline__ C cscale(C a, T s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
+template <typename C> __device__ __forceinline__ C cconj(C a) { C r; r.x = a.x; r.y = -a.y; return r; }
+// (DIR*i) * v ; DIR = -1 forward, +1 inverse
+template <int DIR, typename C> __device__ __forceinline__ C mul_dir_i(C v) {
+  C r;
+  if (DIR < 0) { r.x = v.y; r.y = -v.x; } else { r.x = -v.y; r.y = v.x; }
+  return r;
+}
+// v * (c + i s)
+template <typename C, typename T> __device__ __forceinline__ C cmul_cs(C v, T c, T s) {
+  C r; r.x = v.x * c - v.y * s; r.y = v.x * s + v.y * c; return r;
+}
+// v * w (forward twiddle) or v * conj(w) (inverse)
+template <int DIR, typename C> __device__ __forceinline__ C cmul_tw(C v, C w) {
+  C r;
+  if (DIR < 0) { r.x = v.x * w.x - v.y * w.y; r.y = v.x * w.y + v.y * w.x; }
+  else         { r.x = v.x * w.x + v.y * w.y; r.y = v.y * w.x - v.x * w.y; }
+  return r;
+}
+
+// cos and sin of m*pi/8 (exact mathematical constants).
+__host__ __device__ constexpr double cos_pi8(int m) {
+  return (m & 15) == 0 ? 1.0 : (m & 15) == 1 ? 0.92387953251128674 : (m & 15) == 2 ? 0.70710678118654752
+       : (m & 15) == 3 ? 0.38268343236508977 : (m & 15) == 4 ? 0.0 : (m & 15) == 5 ? -0.38268343236508977
+       : (m & 15) == 6 ? -0.70710678118654752 : (m & 15) == 7 ? -0.92387953251128674 : (m & 15) == 8 ? -1.0
+       : (m & 15) == 9 ? -0.92387953251128674 : (m & 15) == 10 ? -0.70710678118654752
+       : (m & 15) == 11 ? -0.38268343236508977 : (m & 15) == 12 ? 0.0 : (m & 15) == 13 ? 0.38268343236508977
+       : (m & 15) == 14 ? 0.70710678118654752 : 0.92387953251128674;
+}
+__host__ __device__ constexpr double sin_pi8(int m) { return cos_pi8(m - 4); }
+
+// v * exp(DIR * 2*pi*i * m / 16) for a compile-time m.
+template <int DIR, int M, typename C> __device__ __forceinline__ C rot16(C v) {
+  typedef decltype(v.x) T;
+  constexpr int m = ((M % 16) + 16) % 16;
+  if (m == 0) return v;
+  if (m == 8) { C r; r.x = -v.x; r.y = -v.y; return r; }
+  if (m == 4) return mul_dir_i<DIR>(v);
+  if (m == 12) return mul_dir_i<-DIR>(v);
+  constexpr double c = cos_pi8(m);  // angle 2*pi*m/16 = m*pi/8
+  constexpr double s = (DIR < 0 ? -1.0 : 1.0) * sin_pi8(m);
+  return cmul_cs(v, (T)c, (T)s);
+}
+
+template <int DIR, typename C> __device__ __forceinline__ void dft2(C& a, C& b) {
+  C t = a; a = cadd(t, b); b = csub(t, b);
+}
+// natural-order in place DFT-4 of (a0, a1, a2, a3)
+template <int DIR, typename C> __device__ __forceinline__ void dft4(C& a0, C& a1, C& a2, C& a3) {
+  C s02 = cadd(a0, a2), d02 = csub(a0, a2), s13 = cadd(a1, a3), d13 = mul_dir_i<DIR>(csub(a1, a3));
+  a0 = cadd(s02, s13); a2 = csub(s02, s13); a1 = cadd(d02, d13); a3 = csub(d02, d13);
+}
+
+// DFT-R on v[0..R) (stride 1), natural order output.
+template <int R, int DIR, typename C> struct DFT;
+template <int DIR, typename C> struct DFT<2, DIR, C> {
+  static __device__ __forceinline__ void run(C* v) { dft2<DIR>(v[0], v[1]); }
+};
+template <int DIR, typename C> struct DFT<4, DIR, C> {
+  static __device__ __forceinline__ void run(C* v) { dft4<DIR>(v[0], v[1], v[2], v[3]); }
+};
+// 8 = 2 (inner, over n1) x 4 (outer, over n2): X[k1 + 2 k2]
+template <int DIR, typename C> struct DFT<8, DIR, C> {
+  static __device__ __forceinline__ void run(C* v) {
+    dft2<DIR>(v[0], v[4]); dft2<DIR>(v[1], v[5]); dft2<DIR>(v[2], v[6]); dft2<DIR>(v[3], v[7]);
+    // y[n2][k1] : k1=0 -> v[n2], k1=1 -> v[4+n2]; twiddle w8^(n2*k1) = w16^(2*n2)
+    v[5] = rot16<DIR, 2>(v[5]); v[6] = rot16<DIR, 4>(v[6]); v[7] = rot16<DIR, 6>(v[7]);
+    dft4<DIR>(v[0], v[1], v[2], v[3]);   // k1 = 0 -> X[0,2,4,6]
+    dft4<DIR>(v[4], v[5], v[6], v[7]);   // k1 = 1 -> X[1,3,5,7]
+    C t[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) t[i] = v[i];
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) { v[2 * k2] = t[k2]; v[2 * k2 + 1] = t[4 + k2]; }
+  }
+};
+// 16 = 4 (inner, over n1) x 4 (outer, over n2): X[k1 + 4 k2]
+template <int DIR, typename C> struct DFT<16, DIR, C> {
+  static __device__ __forceinline__ void run(C* v) {
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) dft4<DIR>(v[n2], v[n2 + 4], v[n2 + 8], v[n2 + 12]);
+    // y[n2][k1] now in v[n2 + 4*k1]; twiddle by w16^(n2*k1)
+    v[5] = rot16<DIR, 1>(v[5]);  v[6] = rot16<DIR, 2>(v[6]);  v[7] = rot16<DIR, 3>(v[7]);
+    v[9] = rot16<DIR, 2>(v[9]);  v[10] = rot16<DIR, 4>(v[10]); v[11] = rot16<DIR, 6>(v[11]);
+    v[13] = rot16<DIR, 3>(v[13]); v[14] = rot16<DIR, 6>(v[14]); v[15] = rot16<DIR, 9>(v[15]);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) dft4<DIR>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+    // X[k1 + 4 k2] = v[4 k1 + k2]: transpose 4x4
+    C t[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) t[i] = v[i];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+      for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = t[4 * k1 + k2];
+  }
+};
+
+constexpr int FFT_E = 16;  // complex values per thread
+
+// Radix schedule for N with E = 16: NB16 radix-16 stages plus one radix
+// REM stage (REM = 1 means none).  Forward order puts REM last; inverse
+// order puts REM first, so that inverse-last and forward-first radices are
+// both 16 and the row pass can chain them through registers.
+template <int N> struct Sched {
+  static constexpr int log2n = (N <= 1) ? 0 : 1 + Sched<N / 2>::log2n;
+  static constexpr int NB16 = log2n / 4;
+  static constexpr int REM = 1 << (log2n % 4);
+  static constexpr int NSTAGES = NB16 + (REM > 1 ? 1 : 0);
+  static constexpr int TPL = N / FFT_E;  // threads per line
+};
+template <> struct Sched<1> { static constexpr int log2n = 0; };
+
+__host__ __device__ constexpr int smem_pad(int i) { return i + (i >> 4); }
+// line stride in elements: padded length rounded to 32, plus 2 (see bank notes)
+__host__ __device__ constexpr int line_stride(int n) { return ((smem_pad(n - 1) + 1 + 31) / 32) * 32 + 2; }
+
+template <typename C> __device__ __forceinline__ C ldtw(const C* __restrict__ tw, int m) { return __ldg(tw + m); }
+
+// One Stockham stage.  Input: v[] holds this stage's read pattern
+// (x[j + r*N/R]).  Twiddle + DFT in registers.  Output written to the
+// line in shared memory with the Stockham write pattern (STORE=true), or
+// left in registers (last stage).
+template <int N, int R, int NS, int DIR, typename C>
+__device__ __forceinline__ void stage_compute(C* v, int t, const C* __restrict__ tw) {
+  constexpr int E = FFT_E;
+#pragma unroll
+  for (int q = 0; q < E / R; ++q) {
+    const int j = t + q * (N / E);
+    if (NS > 1) {
+      const int k = j % NS;
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[q * R + r] = cmul_tw<DIR>(v[q * R + r], ldtw(tw, r * k * (N / (NS * R))));
+    }
+    DFT<R, DIR, C>::run(v + q * R);
+  }
+}
+template <int N, int R, int NS, typename C>
+__device__ __forceinline__ void stage_store(const C* v, int t, C* line) {
+  constexpr int E = FFT_E;
+#pragma unroll
+  for (int q = 0; q < E / R; ++q) {
+    const int j = t + q * (N / E);
+    const int k = j % NS;
+    const int base = (j / NS) * NS * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) line[smem_pad(base + r * NS)] = v[q * R + r];
+  }
+}
+template <int N, int R, typename C>
+__device__ __forceinline__ void stage_load(C* v, int t, const C* line) {
+  constexpr int E = FFT_E;
+#pragma unroll
+  for (int q = 0; q < E / R; ++q) {
+    const int j = t + q * (N / E);
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[q * R + r] = line[smem_pad(j + r * (N / R))];
+  }
+}
+
+// Position of register v[q*R + r] for a first/last stage of radix R.
+template <int N, int R> __device__ __forceinline__ int reg_pos(int t, int idx) {
+  return t + (idx / R) * (N / FFT_E) + (idx % R) * (N / R);
+}
+
+// Radix of stage s of an N-point transform in direction DIR.
+template <int N, int DIR> __host__ __device__ constexpr int stage_radix(int s) {
+  return (Sched<N>::REM > 1)
+             ? ((DIR > 0) ? (s == 0 ? Sched<N>::REM : 16) : (s == Sched<N>::NSTAGES - 1 ? Sched<N>::REM : 16))
+             : 16;
+}
+
+// Full transform of one line.  On entry v[] holds the first stage's read
+// pattern; on exit v[] holds the result in the last stage's pattern.
+// `line` is this line's shared-memory buffer.  Every thread of the block
+// must call this: it contains __syncthreads().
+template <int N, int DIR, typename C>
+__device__ __forceinline__ void fft_line(C* v, int t, C* line, const C* __restrict__ tw) {
+  constexpr int NST = Sched<N>::NSTAGES;
+  static_assert(NST >= 1 && NST <= 3, "FFT length must be 16..4096");
+  constexpr int R0 = stage_radix<N, DIR>(0);
+  constexpr int R1 = stage_radix<N, DIR>(NST > 1 ? 1 : 0);
+  constexpr int R2 = stage_radix<N, DIR>(NST > 2 ? 2 : 0);
+  stage_compute<N, R0, 1, DIR>(v, t, tw);
+  if (NST > 1) {
+    __syncthreads();
+    stage_store<N, R0, 1>(v, t, line);
+    __syncthreads();
+    stage_load<N, R1>(v, t, line);
+    stage_compute<N, R1, R0, DIR>(v, t, tw);
+  }
+  if (NST > 2) {
+    __syncthreads();
+    stage_store<N, R1, R0>(v, t, line);
+    __syncthreads();
+    stage_load<N, R2>(v, t, line);
+    stage_compute<N, R2, R0 * R1, DIR>(v, t, tw);
+  }
+}
+
+template <int N, int DIR> struct FirstRadix {
+  static constexpr int value = (Sched<N>::REM > 1 && DIR > 0) ? Sched<N>::REM : 16;
+};
+template <int N, int DIR> struct LastRadix {
+  static constexpr int value = (Sched<N>::REM > 1 && DIR < 0) ? Sched<N>::REM : 16;
+};
+
+}  // namespace ptf

@@ -1,0 +1,23 @@
+// Internal declarations shared by the translation units of libptf.so.
+#pragma once
+#include <cuda_runtime.h>
+#include "ptf_pass2d.cuh"
+
+namespace ptf {
+
+// Pass launchers (defined in ptf_kern2d_f64.cu / ptf_kern2d_f32.cu).
+// Column pass: grid (nbx, batch), nbx*W columns, W columns per block.
+template <typename T> cudaError_t launch_col2d(int ny, const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st);
+// Row pass: grid (nby, batch), P row pairs per block.
+template <typename T> cudaError_t launch_row2d(int nx, const RowArgs<T>& a, int P, int nby, int batch, cudaStream_t st);
+// Largest W / P that a launch may use for a given length (shared-memory bound).
+template <typename T> int max_lines_per_block(int n, bool col);
+
+// Element conversions (ptf_util.cu).
+template <typename T> cudaError_t launch_real_in(const double* src, T* dst, long long n, double scale, cudaStream_t st);
+template <typename T> cudaError_t launch_real_out(const T* src, double* dst, long long n, cudaStream_t st);
+// user spectral layout (nkr complex per row) <-> pitched internal layout
+template <typename T> cudaError_t launch_spec_in(const double2* src, typename cplx_of<T>::type* dst, int nkr, int pitch, long long rows, cudaStream_t st);
+template <typename T> cudaError_t launch_spec_out(const typename cplx_of<T>::type* src, double2* dst, int nkr, int pitch, long long rows, cudaStream_t st);
+
+}  // namespace ptf

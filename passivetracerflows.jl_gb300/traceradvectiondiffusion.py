@@ -1,0 +1,384 @@
+"""TracerAdvectionDiffusion: the reference module's user-facing API over libptf.so.
+
+Mirrors ``src/traceradvectiondiffusion.jl`` of PassiveTracerFlows.jl:
+
+=============================================  ==========================================
+reference (Julia)                              here (Python)
+=============================================  ==========================================
+``TwoDAdvectingFlow(; u, v, steadyflow)``      ``TwoDAdvectingFlow(u=..., v=..., steadyflow=...)``
+``Problem(dev, flow; nx, Lx, ..., κ, dt, ...)`` ``Problem(GPU(), flow, nx=..., κ=..., dt=...)``
+``stepforward!(prob, n)``                      ``stepforward(prob, n)``
+``set_c!(prob, c)``                            ``set_c(prob, c)``
+``updatevars!(prob)``                          ``updatevars(prob)``
+``prob.vars.c`` / ``prob.sol`` / ``prob.clock`` same attributes
+=============================================  ==========================================
+
+Arrays use NumPy C order with x the last axis, which is byte-identical to the
+reference's column-major ``(nx, ny[, nz])`` arrays.  All numerics run in the
+CUDA library; this module only converts arguments, evaluates user flow
+functions on the grid (as the reference's broadcasts do) and keeps the
+``vars.c`` mirror.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import math
+from dataclasses import dataclass
+from typing import Callable
+
+import numpy as np
+
+from . import _lib as L
+
+__all__ = [
+    "CPU", "GPU", "noflow", "OneDAdvectingFlow", "TwoDAdvectingFlow", "ThreeDAdvectingFlow",
+    "TwoDGrid", "ThreeDGrid", "gridpoints", "Problem", "set_c", "updatevars", "stepforward",
+]
+
+
+class CPU:
+    """FourierFlows ``CPU()`` device marker.  This package has no CPU path."""
+
+
+class GPU:
+    """FourierFlows ``GPU()`` device marker (the CUDA device of the library)."""
+
+
+def noflow(*args):
+    """``noflow(args...) = 0.0`` (``src/traceradvectiondiffusion.jl:31``)."""
+    return 0.0
+
+
+@dataclass
+class AdvectingFlow:
+    """Common base of the advecting-flow containers (``:29``)."""
+    u: Callable = noflow
+    v: Callable = noflow
+    w: Callable = noflow
+    steadyflow: bool = True
+    dim: int = 2
+
+    def __iter__(self):  # Base.iterate over the fields (``:108-109``)
+        fields = {1: (self.u, self.steadyflow), 2: (self.u, self.v, self.steadyflow),
+                  3: (self.u, self.v, self.w, self.steadyflow)}[self.dim]
+        return iter(fields)
+
+
+def OneDAdvectingFlow(*, u=noflow, steadyflow=True):
+    """``OneDAdvectingFlow(; u=noflow, steadyflow=true)`` (``:54``)."""
+    return AdvectingFlow(u=u, steadyflow=steadyflow, dim=1)
+
+
+def TwoDAdvectingFlow(*, u=noflow, v=noflow, steadyflow=True):
+    """``TwoDAdvectingFlow(; u=noflow, v=noflow, steadyflow=true)`` (``:79``)."""
+    return AdvectingFlow(u=u, v=v, steadyflow=steadyflow, dim=2)
+
+
+def ThreeDAdvectingFlow(*, u=noflow, v=noflow, w=noflow, steadyflow=True):
+    """``ThreeDAdvectingFlow(; u, v, w, steadyflow=true)`` (``:106``)."""
+    return AdvectingFlow(u=u, v=v, w=w, steadyflow=steadyflow, dim=3)
+
+
+class _Grid:
+    """Host-side description of the FourierFlows grid the library uses:
+    ``x = -L/2 + i L/n``, ``kr = 2π/Lx [0..nx/2]``, ``l, m`` in FFT order."""
+
+    def __init__(self, dim, nx, Lx, ny=None, Ly=None, nz=None, Lz=None):
+        self.dim = dim
+        self.nx, self.Lx = int(nx), float(Lx)
+        self.ny = int(ny if ny is not None else nx)
+        self.Ly = float(Ly if Ly is not None else Lx)
+        self.nz = int(nz if nz is not None else nx) if dim == 3 else 1
+        self.Lz = float(Lz if Lz is not None else Lx) if dim == 3 else 0.0
+        self.dx, self.dy = self.Lx / self.nx, self.Ly / self.ny
+        self.x = -self.Lx / 2 + self.dx * np.arange(self.nx)
+        self.y = -self.Ly / 2 + self.dy * np.arange(self.ny)
+        self.nkr = self.nx // 2 + 1
+        self.kr = 2 * np.pi / self.Lx * np.arange(self.nkr)
+        self.l = 2 * np.pi / self.Ly * np.fft.fftfreq(self.ny, 1.0 / self.ny)
+        if dim == 3:
+            self.dz = self.Lz / self.nz
+            self.z = -self.Lz / 2 + self.dz * np.arange(self.nz)
+            self.m = 2 * np.pi / self.Lz * np.fft.fftfreq(self.nz, 1.0 / self.nz)
+            self.shape = (self.nz, self.ny, self.nx)
+        else:
+            self.shape = (self.ny, self.nx)
+        self.spec_shape = self.shape[:-1] + (self.nkr,)
+        self.device = GPU()
+
+    @property
+    def Krsq(self):
+        if self.dim == 3:
+            return self.kr[None, None, :] ** 2 + self.l[None, :, None] ** 2 + self.m[:, None, None] ** 2
+        return self.kr[None, :] ** 2 + self.l[:, None] ** 2
+
+
+def TwoDGrid(dev=None, *, nx, Lx, ny=None, Ly=None):
+    """FourierFlows ``TwoDGrid(dev; nx, Lx, ny, Ly)`` (host-side description)."""
+    return _Grid(2, nx, Lx, ny, Ly)
+
+
+def ThreeDGrid(dev=None, *, nx, Lx, ny=None, Ly=None, nz=None, Lz=None):
+    """FourierFlows ``ThreeDGrid(dev; nx, Lx, ny, Ly, nz, Lz)`` (host-side description)."""
+    return _Grid(3, nx, Lx, ny, Ly, nz, Lz)
+
+
+def gridpoints(grid: _Grid):
+    """FourierFlows ``gridpoints(grid)``: full coordinate arrays, x fastest."""
+    if grid.dim == 3:
+        Z, Y, X = np.meshgrid(grid.z, grid.y, grid.x, indexing="ij")
+        return X, Y, Z
+    Y, X = np.meshgrid(grid.y, grid.x, indexing="ij")
+    return X, Y
+
+
+@dataclass
+class Params:
+    """``ConstDiff{Steady,TimeVarying}FlowParams`` (``:268-452``)."""
+    κ: float
+    η: float
+    ι: float
+    κh: float
+    nκh: int
+    u: object
+    v: object
+    w: object
+    steadyflow: bool
+
+
+@dataclass
+class Vars:
+    """``Vars2D/3D`` (``:597-668``): the physical concentration mirror."""
+    c: np.ndarray
+
+
+class Clock:
+    """FourierFlows ``Clock``: ``t``, ``dt``, ``step`` read from the library."""
+
+    def __init__(self, prob):
+        self._prob = prob
+
+    def _read(self):
+        t, s = ct.c_double(), ct.c_int64()
+        L.check(L.load().ptf_clock(self._prob._h, ct.byref(t), ct.byref(s)), self._prob._h)
+        return t.value, s.value
+
+    @property
+    def t(self):
+        return self._read()[0]
+
+    @property
+    def step(self):
+        return self._read()[1]
+
+    @property
+    def dt(self):
+        return self._prob._cfg.dt
+
+
+def _kw(kwargs, names, default):
+    for n in names:
+        if n in kwargs:
+            return kwargs.pop(n)
+    return default
+
+
+def _eval_on_grid(f, shape, pts, *extra):
+    return np.ascontiguousarray(np.broadcast_to(np.asarray(f(*pts, *extra), dtype=np.float64), shape))
+
+
+class Problem:
+    """``TracerAdvectionDiffusion.Problem(dev, advecting_flow; nx=128, Lx=2π, ny=nx,
+    Ly=Lx, [nz=nx, Lz=Lx,] κ=0.1, η=κ, [ι=κ,] dt=0.01, stepper="RK4", T=Float64)``
+    (``src/traceradvectiondiffusion.jl:165-216``).
+
+    Extensions (keyword-only): ``κh``/``nκh`` (hyperdiffusion, reachable in the
+    reference only through ``ConstDiffSteadyFlowParams``), ``batch`` (independent
+    solves sharing grid, parameters and flow), ``time_mode`` ("clock" as the
+    reference, or "stage").  ``T=np.float32`` selects the FP32 form.
+    """
+
+    def __init__(self, dev, advecting_flow: AdvectingFlow, **kwargs):
+        if isinstance(dev, CPU) or dev is CPU:
+            raise NotImplementedError("this package runs on the GPU only: pass GPU()")
+        flow = advecting_flow
+        if not isinstance(flow, AdvectingFlow):
+            raise TypeError("advecting_flow must be a OneD/TwoD/ThreeDAdvectingFlow")
+        dim = flow.dim
+        nx = int(kwargs.pop("nx", 128))
+        Lx = float(kwargs.pop("Lx", 2 * math.pi))
+        ny = int(kwargs.pop("ny", nx))
+        Ly = float(kwargs.pop("Ly", Lx))
+        nz = int(kwargs.pop("nz", nx))
+        Lz = float(kwargs.pop("Lz", Lx))
+        κ = float(_kw(kwargs, ("κ", "kappa"), 0.1))
+        η = float(_kw(kwargs, ("η", "eta"), κ))
+        ι = float(_kw(kwargs, ("ι", "iota"), κ))
+        κh = float(_kw(kwargs, ("κh", "kappah"), 0.0))
+        nκh = int(_kw(kwargs, ("nκh", "nkappah"), 0))
+        dt = float(kwargs.pop("dt", 0.01))
+        stepper = kwargs.pop("stepper", "RK4")
+        T = kwargs.pop("T", np.float64)
+        batch = int(kwargs.pop("batch", 1))
+        time_mode = kwargs.pop("time_mode", "clock")
+        if kwargs:
+            raise TypeError(f"unexpected keyword arguments: {sorted(kwargs)}")
+        steppers = {"RK4": L.PTF_RK4, "ETDRK4": L.PTF_ETDRK4}
+        if stepper not in steppers:
+            raise ValueError(f"stepper {stepper!r} is not supported (RK4, ETDRK4)")
+        if T in (np.float64, float, "Float64"):
+            prec = L.PTF_FP64
+        elif T in (np.float32, "Float32"):
+            prec = L.PTF_FP32
+        else:
+            raise ValueError("T must be np.float64 or np.float32")
+        lib = L.load()
+        cfg = L.PtfConfig()
+        lib.ptf_config_default(ct.byref(cfg), dim)
+        cfg.nx, cfg.ny, cfg.nz = nx, ny, nz
+        cfg.Lx, cfg.Ly, cfg.Lz = Lx, Ly, Lz
+        cfg.kappa, cfg.eta, cfg.iota = κ, η, ι
+        cfg.kappah, cfg.nkappah = κh, nκh
+        cfg.dt = dt
+        cfg.stepper = steppers[stepper]
+        cfg.precision = prec
+        cfg.time_mode = {"clock": L.PTF_CLOCK_T, "stage": L.PTF_STAGE_T}[time_mode]
+        cfg.batch = batch
+        h = ct.c_void_p()
+        L.check(lib.ptf_create(ct.byref(cfg), ct.byref(h)), None)
+        self._h = h
+        self._cfg = cfg
+        self.grid = _Grid(dim, nx, Lx, ny, Ly, nz, Lz)
+        self.batch = batch
+        self.stepper = stepper
+        self.params = Params(κ, η, ι, κh, nκh, flow.u, flow.v, flow.w, flow.steadyflow)
+        self.flow = flow
+        shape = ((batch,) if batch > 1 else ()) + self.grid.shape
+        self.vars = Vars(np.zeros(shape))
+        self.clock = Clock(self)
+        if flow.steadyflow:
+            pts = gridpoints(self.grid)
+            comps = (flow.u, flow.v, flow.w)[:dim]
+            self.set_flow_arrays(*[_eval_on_grid(f, self.grid.shape, pts) for f in comps])
+        else:
+            self._flow_t = None
+
+    # -- library plumbing ------------------------------------------------------------
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                L.load().ptf_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def set_flow_arrays(self, *vel):
+        """Set the flow from grid arrays (host NumPy or torch CUDA tensors)."""
+        arrs = []
+        where = L.PTF_HOST
+        ptrs = []
+        for a in vel:
+            if hasattr(a, "is_cuda") and a.is_cuda:
+                where = L.PTF_DEVICE
+                ptrs.append(ct.c_void_p(a.data_ptr()))
+                arrs.append(a)
+            else:
+                a = np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64), self.grid.shape))
+                arrs.append(a)
+                ptrs.append(a.ctypes.data_as(ct.c_void_p))
+        while len(ptrs) < 3:
+            ptrs.append(None)
+        L.check(L.load().ptf_set_flow_arrays(self._h, ptrs[0], ptrs[1], ptrs[2], where), self._h)
+
+    def _refresh_flow(self):
+        """Time-varying flow at ``clock.t`` (``:715-718``), evaluated once per step."""
+        t = self.clock.t
+        if self._flow_t == t:
+            return
+        pts = gridpoints(self.grid)
+        comps = (self.flow.u, self.flow.v, self.flow.w)[: self.grid.dim]
+        self.set_flow_arrays(*[_eval_on_grid(f, self.grid.shape, pts, t) for f in comps])
+        self._flow_t = t
+
+    @property
+    def sol(self):
+        """``prob.sol``: the spectral state, complex ``(ny, nx/2+1)`` (C order)."""
+        shape = ((self.batch,) if self.batch > 1 else ()) + self.grid.spec_shape
+        out = np.empty(shape, dtype=np.complex128)
+        L.check(L.load().ptf_get_sol(self._h, out.ctypes.data_as(ct.c_void_p), L.PTF_HOST), self._h)
+        return out
+
+    @sol.setter
+    def sol(self, value):
+        shape = ((self.batch,) if self.batch > 1 else ()) + self.grid.spec_shape
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(value, dtype=np.complex128), shape))
+        L.check(L.load().ptf_set_sol(self._h, a.ctypes.data_as(ct.c_void_p), L.PTF_HOST), self._h)
+
+    def calcN(self, sol):
+        """The ``calcN!`` plugin (``:756-786``): ``N = rfft(-(u·∇c))`` for ``sol``."""
+        shape = ((self.batch,) if self.batch > 1 else ()) + self.grid.spec_shape
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(sol, dtype=np.complex128), shape))
+        out = np.empty(shape, dtype=np.complex128)
+        if not self.flow.steadyflow:
+            self._refresh_flow()
+        L.check(L.load().ptf_calcN(self._h, a.ctypes.data_as(ct.c_void_p), out.ctypes.data_as(ct.c_void_p),
+                                   L.PTF_HOST), self._h)
+        return out
+
+    def synchronize(self):
+        L.check(L.load().ptf_synchronize(self._h), self._h)
+
+    @property
+    def stream(self):
+        p = ct.c_void_p()
+        L.check(L.load().ptf_get_stream(self._h, ct.byref(p)), self._h)
+        return p.value
+
+    @property
+    def device_bytes(self):
+        b = ct.c_int64()
+        L.check(L.load().ptf_device_bytes(self._h, ct.byref(b)), self._h)
+        return b.value
+
+    @property
+    def kernel_launches(self):
+        b = ct.c_int64()
+        L.check(L.load().ptf_kernel_launches(self._h, ct.byref(b)), self._h)
+        return b.value
+
+
+def set_c(prob: Problem, c):
+    """``set_c!(prob, c)`` (``:844-852, :872``): ``sol = rfft(c)``, then ``updatevars!``."""
+    if hasattr(c, "is_cuda") and c.is_cuda:
+        if c.dtype != __import__("torch").float64 or not c.is_contiguous():
+            raise ValueError("device fields must be contiguous float64 tensors")
+        L.check(L.load().ptf_set_c(prob._h, ct.c_void_p(c.data_ptr()), L.PTF_DEVICE), prob._h)
+    else:
+        shape = ((prob.batch,) if prob.batch > 1 else ()) + prob.grid.shape
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(c, dtype=np.float64), shape))
+        L.check(L.load().ptf_set_c(prob._h, a.ctypes.data_as(ct.c_void_p), L.PTF_HOST), prob._h)
+    updatevars(prob)
+
+
+def updatevars(prob: Problem):
+    """``updatevars!(prob)`` (``:815-821, :837``): ``vars.c = irfft(sol)``."""
+    out = prob.vars.c
+    L.check(L.load().ptf_get_c(prob._h, out.ctypes.data_as(ct.c_void_p), L.PTF_HOST), prob._h)
+
+
+def stepforward(prob: Problem, nsteps: int = 1):
+    """FourierFlows ``stepforward!(prob, nsteps)``: ``nsteps`` stepper updates,
+    each followed by ``clock.t += dt`` and ``clock.step += 1``.  A time-varying
+    flow is re-evaluated at ``clock.t`` before every step, as the reference's
+    ``calcN!`` does for all four stages of a step (``:715-718``)."""
+    nsteps = int(nsteps)
+    if nsteps < 0:
+        raise ValueError("nsteps must be non-negative")
+    lib = L.load()
+    if prob.flow.steadyflow:
+        L.check(lib.ptf_step(prob._h, nsteps), prob._h)
+        return
+    for _ in range(nsteps):
+        prob._refresh_flow()
+        L.check(lib.ptf_step(prob._h, 1), prob._h)

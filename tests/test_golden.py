@@ -1,0 +1,35 @@
+"""The oracle reproduces its committed golden fixtures (CPU)."""
+from pathlib import Path
+
+import numpy as np
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def _mod():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", GOLD / "make_golden.py")
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m
+
+
+def test_golden_cellular128_rk4(oracle):
+    g = np.load(GOLD / "cellular128_rk4.npz")
+    d = _mod().cellular128_rk4()
+    for k in ("c100", "c2000"):
+        assert oracle.rel_l2(d[k], g[k]) <= 1e-13, k
+    assert int(g["step"]) == 2000 and abs(float(g["t"]) - 20.0) < 1e-9
+
+
+def test_golden_cellular128_etdrk4(oracle):
+    g = np.load(GOLD / "cellular128_etdrk4.npz")
+    d = _mod().cellular128_etdrk4()
+    assert oracle.rel_l2(d["c50"], g["c50"]) <= 1e-13
+
+
+def test_golden_mass_conservation(oracle):
+    """Incompressible advection + diffusion conserve Σc up to aliasing round-off."""
+    g = np.load(GOLD / "cellular128_rk4.npz")
+    m0, m1 = g["c0"].sum(), g["c2000"].sum()
+    assert abs(m1 - m0) / abs(m0) < 1e-12

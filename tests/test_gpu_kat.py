@@ -1,0 +1,22 @@
+"""The reference's own known-answer tests run through the GPU path, at the
+reference's tolerances (and at the tighter bounds the oracle reaches)."""
+import pytest
+
+import kat
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name,tight", [
+    ("constvel2D", 2e-8), ("timedependentvel2D", 1e-10), ("diffusion2D", 1e-9), ("hyperdiffusion", 1e-9),
+])
+@pytest.mark.parametrize("stepper", ["RK4", "ETDRK4"])
+def test_reference_kat_2d_gpu(gpu, name, tight, stepper):
+    err, rtol = getattr(kat, name)(gpu, gpu.GPU(), stepper=stepper)
+    assert err <= rtol, f"{name}: {err:.3e} > reference rtol {rtol:.3e}"
+    assert err <= tight
+
+
+def test_diffusion2D_timevarying_gpu(gpu):
+    err, rtol = kat.diffusion2D(gpu, gpu.GPU(), steadyflow=False)
+    assert err <= rtol and err <= 1e-9
