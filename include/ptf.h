@@ -127,6 +127,30 @@ int ptf_profile_read(ptf_handle* h, int32_t kind, double* total_ms, int64_t* lau
 int ptf_kernel_launches(const ptf_handle* h, int64_t* count);
 int32_t ptf_abi_version(void);
 
+/* Size of the fixed device scratch used by ptf_calcN2d_noalloc (16 MiB). */
+#define PTF_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* No counterpart in the reference: the reference's calcN! always works in
+ * the Vars buffers its Problem allocated.  This is the same advective term
+ * as ptf_calcN (N = rfft(-(u c_x + v c_y)) for one 2D FP64 spectral field)
+ * for callers that must not have a library allocate device memory: a host
+ * whose own memory pool owns the whole device (a Julia process under
+ * CUDA.jl's pool, for instance) or a time-critical loop that cannot take
+ * the device-wide synchronisation of cudaFree.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine.
+ *   sol, N: device, (nx/2+1)*ny complex doubles, column-major (x fastest)
+ *   u, v:   device, nx*ny doubles (the flow on the grid, unscaled)
+ *   stream: cudaStream_t the work is ordered on (NULL: legacy default stream)
+ * Intermediates live in one file-scope device array of
+ * PTF_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until
+ * exit; grids needing more (1024x1024 and larger) are rejected with
+ * PTF_ERR_MEMORY.  The first call on a device does a one-time set-up (symbol
+ * address lookup and a synchronous twiddle upload); make it before any
+ * stream capture.  All calls share that array and it keeps the last call's
+ * contents, so calls that overlap on the GPU race.  Errors: ptf_last_error(NULL). */
+int ptf_calcN2d_noalloc(int32_t nx, int32_t ny, double Lx, double Ly, const double* sol, const double* u,
+                        const double* v, double* N, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

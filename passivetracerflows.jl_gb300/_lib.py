@@ -63,6 +63,8 @@ SIGNATURES = {
     "ptf_set_stream": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
     "ptf_device_bytes": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_int64)]),
     "ptf_kernel_launches": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_int64)]),
+    "ptf_calcN2d_noalloc": (ct.c_int, [ct.c_int32, ct.c_int32, ct.c_double, ct.c_double, ct.c_void_p, ct.c_void_p,
+                                       ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "ptf_profile": (ct.c_int, [ct.c_void_p, ct.c_int32]),
     "ptf_profile_read": (ct.c_int, [ct.c_void_p, ct.c_int32, ct.POINTER(ct.c_double), ct.POINTER(ct.c_int64),
                                     ct.POINTER(ct.c_double)]),

@@ -84,6 +84,8 @@ template <typename F> void parallel_for(long long n, F f) {
 
 }  // namespace
 
+void ptf::set_global_error(const std::string& msg) { g_create_error = msg; }
+
 struct ptf_handle {
   ptf_config cfg;
   int nkr = 0, pitch = 0;

@@ -3,7 +3,12 @@
 #include <cuda_runtime.h>
 #include "ptf_pass2d.cuh"
 
+#include <string>
+
 namespace ptf {
+
+// Message returned by ptf_last_error(NULL) (calls without a handle).
+void set_global_error(const std::string& msg);
 
 // Pass launchers (defined in ptf_kern2d_f64.cu / ptf_kern2d_f32.cu).
 // Column pass: grid (nbx, batch), nbx*W columns, W columns per block.
