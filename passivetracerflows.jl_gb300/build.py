@@ -30,8 +30,21 @@ def _nvcc() -> str:
     return p
 
 
-def _sources():
-    return sorted(CSRC.glob("*.cu"))
+# Per-(precision, length) instantiation units: one source, many objects.
+INST_SOURCES = {"ptf_k2d_inst.cu": [("float", n) for n in (16, 32, 64, 128, 256, 512, 1024, 2048, 4096)]
+                + [("double", n) for n in (16, 32, 64, 128, 256, 512, 1024, 2048, 4096)]}
+
+
+def _units():
+    """(source, object, extra defines) for every object of the library."""
+    units = []
+    for src in sorted(CSRC.glob("*.cu")):
+        if src.name in INST_SOURCES:
+            for t, n in INST_SOURCES[src.name]:
+                units.append((src, BUILD / f"{src.stem}_{t}_{n}.o", [f"-DPTF_T={t}", f"-DPTF_N={n}"]))
+        else:
+            units.append((src, BUILD / (src.stem + ".o"), []))
+    return units
 
 
 def _deps():
@@ -51,18 +64,20 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> Path:
     BUILD.mkdir(exist_ok=True)
     dep_mtime = max((p.stat().st_mtime for p in _deps()), default=0.0)
     jobs = []
-    for src in _sources():
-        obj = BUILD / (src.stem + ".o")
+    units = _units()
+    for src, obj, defs in units:
         stale = force or not obj.exists() or obj.stat().st_mtime < max(src.stat().st_mtime, dep_mtime)
         if stale:
-            jobs.append((src, obj))
+            jobs.append((src, obj, defs))
     workers = max(1, min(len(jobs), os.cpu_count() or 1))
     if jobs:
+        # the heavy instantiation units first
+        jobs.sort(key=lambda j: (not j[2], -(int(j[2][1].split("=")[1]) if j[2] else 0)))
         with cf.ThreadPoolExecutor(max_workers=workers) as ex:
-            futs = [ex.submit(_compile, nvcc, s, o, extra) for s, o in jobs]
+            futs = [ex.submit(_compile, nvcc, s, o, list(extra) + d) for s, o, d in jobs]
             for f in futs:
                 f.result()
-    objs = [str(BUILD / (s.stem + ".o")) for s in _sources()]
+    objs = [str(o) for _, o, _ in units]
     newest = max(Path(o).stat().st_mtime for o in objs)
     if force or jobs or not LIB.exists() or LIB.stat().st_mtime < newest:
         tmp = LIB.with_suffix(".so.tmp")

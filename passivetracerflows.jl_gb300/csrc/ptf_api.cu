@@ -407,22 +407,10 @@ int ptf_create(const ptf_config* cfg, ptf_handle** out) {
   if (e != cudaSuccess) { ptf_destroy(h); return cuda_fail(nullptr, e, "stream create"); }
   h->own_stream = true;
   // launch shapes
-  {
-    const int wmax = h->fp32 ? max_lines_per_block<float>(c.ny, true) : max_lines_per_block<double>(c.ny, true);
-    int W = h->fp32 ? 4 : 2;
-    const int tply = c.ny / 16;
-    while (W * tply < 64 && W < 8) W *= 2;
-    if (W > wmax) W = wmax;
-    while (h->pitch % W) W /= 2;
-    h->colW = W < 1 ? 1 : W;
-    const int pmax = h->fp32 ? max_lines_per_block<float>(c.nx, false) : max_lines_per_block<double>(c.nx, false);
-    int P = 1;
-    const int tplx = c.nx / 16;
-    while (P * tplx < 64 && P < 16) P *= 2;
-    if (P > pmax) P = pmax;
-    while ((c.ny / 2) % P) P /= 2;
-    h->rowP = P < 1 ? 1 : P;
-  }
+  h->colW = h->fp32 ? default_lines_per_block<float>(c.ny, true, h->pitch)
+                    : default_lines_per_block<double>(c.ny, true, h->pitch);
+  h->rowP = h->fp32 ? default_lines_per_block<float>(c.nx, false, c.ny / 2)
+                    : default_lines_per_block<double>(c.nx, false, c.ny / 2);
   const size_t B = (size_t)c.batch;
   const size_t sc = (size_t)h->plane * B * elem_c(h);
   const size_t sp = (size_t)h->nphys * B * elem_r(h);

@@ -64,6 +64,20 @@ __host__ __device__ constexpr double cos_pi8(int m) {
 }
 __host__ __device__ constexpr double sin_pi8(int m) { return cos_pi8(m - 4); }
 
+// cos of m*pi/16 by symmetry from the first-quadrant values.
+__host__ __device__ constexpr double cos_q16(int k) {  // 0 <= k <= 8
+  return k == 0 ? 1.0 : k == 1 ? 0.98078528040323044 : k == 2 ? 0.92387953251128674 : k == 3 ? 0.83146961230254524
+       : k == 4 ? 0.70710678118654752 : k == 5 ? 0.55557023301960218 : k == 6 ? 0.38268343236508977
+       : k == 7 ? 0.19509032201612826 : 0.0;
+}
+__host__ __device__ constexpr double cos_pi16(int m) {
+  return ((m % 32) + 32) % 32 <= 8 ? cos_q16(((m % 32) + 32) % 32)
+       : ((m % 32) + 32) % 32 <= 16 ? -cos_q16(16 - ((m % 32) + 32) % 32)
+       : ((m % 32) + 32) % 32 <= 24 ? -cos_q16(((m % 32) + 32) % 32 - 16)
+       : cos_q16(32 - ((m % 32) + 32) % 32);
+}
+__host__ __device__ constexpr double sin_pi16(int m) { return cos_pi16(m - 8); }
+
 // v * exp(DIR * 2*pi*i * m / 16) for a compile-time m.
 template <int DIR, int M, typename C> __device__ __forceinline__ C rot16(C v) {
   typedef decltype(v.x) T;
@@ -74,6 +88,16 @@ template <int DIR, int M, typename C> __device__ __forceinline__ C rot16(C v) {
   if (m == 12) return mul_dir_i<-DIR>(v);
   constexpr double c = cos_pi8(m);  // angle 2*pi*m/16 = m*pi/8
   constexpr double s = (DIR < 0 ? -1.0 : 1.0) * sin_pi8(m);
+  return cmul_cs(v, (T)c, (T)s);
+}
+
+// v * exp(DIR * 2*pi*i * m / 32) for a compile-time m.
+template <int DIR, int M, typename C> __device__ __forceinline__ C rot32(C v) {
+  typedef decltype(v.x) T;
+  constexpr int m = ((M % 32) + 32) % 32;
+  if (m % 2 == 0) return rot16<DIR, m / 2>(v);
+  constexpr double c = cos_pi16(m);  // angle 2*pi*m/32 = m*pi/16
+  constexpr double s = (DIR < 0 ? -1.0 : 1.0) * sin_pi16(m);
   return cmul_cs(v, (T)c, (T)s);
 }
 
@@ -131,20 +155,54 @@ template <int DIR, typename C> struct DFT<16, DIR, C> {
   }
 };
 
-constexpr int FFT_E = 16;  // complex values per thread
+// 32 = 4 (inner, over n1; inputs stride 8) x 8 (outer, over n2): X[k1 + 4 k2]
+template <int DIR, typename C> struct DFT<32, DIR, C> {
+  static __device__ __forceinline__ void run(C* v) {
+#pragma unroll
+    for (int n2 = 0; n2 < 8; ++n2) dft4<DIR>(v[n2], v[n2 + 8], v[n2 + 16], v[n2 + 24]);
+    // y[n2][k1] in v[n2 + 8*k1]; twiddle by w32^(n2*k1)
+#define PTF_R32(n2, k1) v[n2 + 8 * k1] = rot32<DIR, n2 * k1>(v[n2 + 8 * k1]);
+    PTF_R32(1, 1) PTF_R32(2, 1) PTF_R32(3, 1) PTF_R32(4, 1) PTF_R32(5, 1) PTF_R32(6, 1) PTF_R32(7, 1)
+    PTF_R32(1, 2) PTF_R32(2, 2) PTF_R32(3, 2) PTF_R32(4, 2) PTF_R32(5, 2) PTF_R32(6, 2) PTF_R32(7, 2)
+    PTF_R32(1, 3) PTF_R32(2, 3) PTF_R32(3, 3) PTF_R32(4, 3) PTF_R32(5, 3) PTF_R32(6, 3) PTF_R32(7, 3)
+#undef PTF_R32
+    // outer DFT-8 over n2 for each k1 (contiguous v[8*k1 .. 8*k1+7]) -> X[k1 + 4 k2] at v[8 k1 + k2]
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) DFT<8, DIR, C>::run(v + 8 * k1);
+    C t[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) t[i] = v[i];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+      for (int k2 = 0; k2 < 8; ++k2) v[k1 + 4 * k2] = t[8 * k1 + k2];
+  }
+};
+
+constexpr int FFT_E = 16;  // default complex values per thread
+
+// Values per thread of the pass kernels: FP32 uses 32 (radix-32 stages:
+// fewer shared-memory exchanges, and its register file allows it); FP64
+// uses 16 (twice the register bytes per value).
+template <typename T, int N> struct PassE { static constexpr int value = 16; };
+template <int N> struct PassE<float, N> { static constexpr int value = 16; };
 
 // Radix schedule for N with E = 16: NB16 radix-16 stages plus one radix
 // REM stage (REM = 1 means none).  Forward order puts REM last; inverse
 // order puts REM first, so that inverse-last and forward-first radices are
 // both 16 and the row pass can chain them through registers.
-template <int N> struct Sched {
-  static constexpr int log2n = (N <= 1) ? 0 : 1 + Sched<N / 2>::log2n;
-  static constexpr int NB16 = log2n / 4;
-  static constexpr int REM = 1 << (log2n % 4);
-  static constexpr int NSTAGES = NB16 + (REM > 1 ? 1 : 0);
-  static constexpr int TPL = N / FFT_E;  // threads per line
+template <int N> struct Log2 { static constexpr int value = 1 + Log2<N / 2>::value; };
+template <> struct Log2<1> { static constexpr int value = 0; };
+// Radix schedule for N with E values per thread: NBE radix-E stages plus one
+// radix-REM stage (REM = 1: none).
+template <int N, int E = FFT_E> struct Sched {
+  static constexpr int log2n = Log2<N>::value;
+  static constexpr int log2e = Log2<E>::value;
+  static constexpr int NBE = log2n / log2e;
+  static constexpr int REM = 1 << (log2n % log2e);
+  static constexpr int NSTAGES = NBE + (REM > 1 ? 1 : 0);
+  static constexpr int TPL = N / E;  // threads per line
 };
-template <> struct Sched<1> { static constexpr int log2n = 0; };
 
 __host__ __device__ constexpr int smem_pad(int i) { return i + (i >> 4); }
 // line stride in elements: padded length rounded to 32, plus 2 (see bank notes)
@@ -156,9 +214,8 @@ template <typename C> __device__ __forceinline__ C ldtw(const C* __restrict__ tw
 // (x[j + r*N/R]).  Twiddle + DFT in registers.  Output written to the
 // line in shared memory with the Stockham write pattern (STORE=true), or
 // left in registers (last stage).
-template <int N, int R, int NS, int DIR, typename C>
+template <int N, int R, int NS, int DIR, int E, typename C>
 __device__ __forceinline__ void stage_compute(C* v, int t, const C* __restrict__ tw) {
-  constexpr int E = FFT_E;
 #pragma unroll
   for (int q = 0; q < E / R; ++q) {
     const int j = t + q * (N / E);
@@ -170,9 +227,8 @@ __device__ __forceinline__ void stage_compute(C* v, int t, const C* __restrict__
     DFT<R, DIR, C>::run(v + q * R);
   }
 }
-template <int N, int R, int NS, typename C>
+template <int N, int R, int NS, int E, typename C>
 __device__ __forceinline__ void stage_store(const C* v, int t, C* line) {
-  constexpr int E = FFT_E;
 #pragma unroll
   for (int q = 0; q < E / R; ++q) {
     const int j = t + q * (N / E);
@@ -182,9 +238,8 @@ __device__ __forceinline__ void stage_store(const C* v, int t, C* line) {
     for (int r = 0; r < R; ++r) line[smem_pad(base + r * NS)] = v[q * R + r];
   }
 }
-template <int N, int R, typename C>
+template <int N, int R, int E, typename C>
 __device__ __forceinline__ void stage_load(C* v, int t, const C* line) {
-  constexpr int E = FFT_E;
 #pragma unroll
   for (int q = 0; q < E / R; ++q) {
     const int j = t + q * (N / E);
@@ -194,50 +249,50 @@ __device__ __forceinline__ void stage_load(C* v, int t, const C* line) {
 }
 
 // Position of register v[q*R + r] for a first/last stage of radix R.
-template <int N, int R> __device__ __forceinline__ int reg_pos(int t, int idx) {
-  return t + (idx / R) * (N / FFT_E) + (idx % R) * (N / R);
+template <int N, int R, int E = FFT_E> __device__ __forceinline__ int reg_pos(int t, int idx) {
+  return t + (idx / R) * (N / E) + (idx % R) * (N / R);
 }
 
-// Radix of stage s of an N-point transform in direction DIR.
-template <int N, int DIR> __host__ __device__ constexpr int stage_radix(int s) {
-  return (Sched<N>::REM > 1)
-             ? ((DIR > 0) ? (s == 0 ? Sched<N>::REM : 16) : (s == Sched<N>::NSTAGES - 1 ? Sched<N>::REM : 16))
-             : 16;
+// Radix of stage s of an N-point transform in direction DIR (E per thread).
+template <int N, int DIR, int E = FFT_E> __host__ __device__ constexpr int stage_radix(int s) {
+  return (Sched<N, E>::REM > 1)
+             ? ((DIR > 0) ? (s == 0 ? Sched<N, E>::REM : E) : (s == Sched<N, E>::NSTAGES - 1 ? Sched<N, E>::REM : E))
+             : E;
 }
 
 // Full transform of one line.  On entry v[] holds the first stage's read
 // pattern; on exit v[] holds the result in the last stage's pattern.
 // `line` is this line's shared-memory buffer.  Every thread of the block
 // must call this: it contains __syncthreads().
-template <int N, int DIR, typename C>
+template <int N, int DIR, int E = FFT_E, typename C>
 __device__ __forceinline__ void fft_line(C* v, int t, C* line, const C* __restrict__ tw) {
-  constexpr int NST = Sched<N>::NSTAGES;
+  constexpr int NST = Sched<N, E>::NSTAGES;
   static_assert(NST >= 1 && NST <= 3, "FFT length must be 16..4096");
-  constexpr int R0 = stage_radix<N, DIR>(0);
-  constexpr int R1 = stage_radix<N, DIR>(NST > 1 ? 1 : 0);
-  constexpr int R2 = stage_radix<N, DIR>(NST > 2 ? 2 : 0);
-  stage_compute<N, R0, 1, DIR>(v, t, tw);
+  constexpr int R0 = stage_radix<N, DIR, E>(0);
+  constexpr int R1 = stage_radix<N, DIR, E>(NST > 1 ? 1 : 0);
+  constexpr int R2 = stage_radix<N, DIR, E>(NST > 2 ? 2 : 0);
+  stage_compute<N, R0, 1, DIR, E>(v, t, tw);
   if (NST > 1) {
     __syncthreads();
-    stage_store<N, R0, 1>(v, t, line);
+    stage_store<N, R0, 1, E>(v, t, line);
     __syncthreads();
-    stage_load<N, R1>(v, t, line);
-    stage_compute<N, R1, R0, DIR>(v, t, tw);
+    stage_load<N, R1, E>(v, t, line);
+    stage_compute<N, R1, R0, DIR, E>(v, t, tw);
   }
   if (NST > 2) {
     __syncthreads();
-    stage_store<N, R1, R0>(v, t, line);
+    stage_store<N, R1, R0, E>(v, t, line);
     __syncthreads();
-    stage_load<N, R2>(v, t, line);
-    stage_compute<N, R2, R0 * R1, DIR>(v, t, tw);
+    stage_load<N, R2, E>(v, t, line);
+    stage_compute<N, R2, R0 * R1, DIR, E>(v, t, tw);
   }
 }
 
-template <int N, int DIR> struct FirstRadix {
-  static constexpr int value = (Sched<N>::REM > 1 && DIR > 0) ? Sched<N>::REM : 16;
+template <int N, int DIR, int E = FFT_E> struct FirstRadix {
+  static constexpr int value = (Sched<N, E>::REM > 1 && DIR > 0) ? Sched<N, E>::REM : E;
 };
-template <int N, int DIR> struct LastRadix {
-  static constexpr int value = (Sched<N>::REM > 1 && DIR < 0) ? Sched<N>::REM : 16;
+template <int N, int DIR, int E = FFT_E> struct LastRadix {
+  static constexpr int value = (Sched<N, E>::REM > 1 && DIR < 0) ? Sched<N, E>::REM : E;
 };
 
 }  // namespace ptf

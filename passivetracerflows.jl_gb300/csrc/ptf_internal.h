@@ -17,6 +17,8 @@ template <typename T> cudaError_t launch_col2d(int ny, const ColArgs<T>& a, int 
 template <typename T> cudaError_t launch_row2d(int nx, const RowArgs<T>& a, int P, int nby, int batch, cudaStream_t st);
 // Largest W / P that a launch may use for a given length (shared-memory bound).
 template <typename T> int max_lines_per_block(int n, bool col);
+// Default W (col) or P (row) for length n; `divisor` must be divisible by it.
+template <typename T> int default_lines_per_block(int n, bool col, int divisor);
 
 // Element conversions (ptf_util.cu).
 template <typename T> cudaError_t launch_real_in(const double* src, T* dst, long long n, double scale, cudaStream_t st);

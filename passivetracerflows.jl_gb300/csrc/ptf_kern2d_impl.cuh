@@ -1,4 +1,6 @@
-// Launch dispatch of the 2D pass kernels over the supported lengths.
+// Launchers of the 2D pass kernels for one (precision, length).  Each pair is
+// explicitly instantiated in its own object (ptf_k2d_inst.cu) so the
+// kernels compile in parallel; ptf_kern2d.cu dispatches over them.
 #pragma once
 #include "ptf_internal.h"
 
@@ -13,75 +15,52 @@ template <typename T, int N> struct PassLaunch {
     if (cudaFuncGetAttributes(&at, kern) != cudaSuccess) return 0;
     return at.maxThreadsPerBlock;
   }
-  static cudaError_t col(const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st) {
-    if (W * (N / FFT_E) > max_threads(col_pass_kernel<T, N>)) return cudaErrorInvalidConfiguration;
-    const size_t smem = (size_t)W * line_bytes();
-    cudaError_t e = cudaFuncSetAttribute(col_pass_kernel<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  template <int MODE> static cudaError_t col_m(const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st) {
+    if (W * pass_tpl<T, N>() > max_threads(col_pass_kernel<T, N, MODE>)) return cudaErrorInvalidConfiguration;
+    const size_t smem = col_smem_bytes<T, N>(W);
+    cudaError_t e = cudaFuncSetAttribute(col_pass_kernel<T, N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    col_pass_kernel<T, N><<<dim3(nbx, batch), dim3(W * (N / FFT_E)), smem, st>>>(a);
+    col_pass_kernel<T, N, MODE><<<dim3(nbx, batch), dim3(W * pass_tpl<T, N>()), smem, st>>>(a);
     return cudaGetLastError();
   }
+  static cudaError_t col(const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st) {
+    switch (a.mode) {
+      case COL_PROLOGUE: return col_m<COL_PROLOGUE>(a, W, nbx, batch, st);
+      case COL_FWD_STORE: return col_m<COL_FWD_STORE>(a, W, nbx, batch, st);
+      case COL_FWD_N: return col_m<COL_FWD_N>(a, W, nbx, batch, st);
+      case COL_RK4_1: return col_m<COL_RK4_1>(a, W, nbx, batch, st);
+      case COL_RK4_2: return col_m<COL_RK4_2>(a, W, nbx, batch, st);
+      case COL_RK4_3: return col_m<COL_RK4_3>(a, W, nbx, batch, st);
+      case COL_RK4_4: return col_m<COL_RK4_4>(a, W, nbx, batch, st);
+      case COL_ETD_1: return col_m<COL_ETD_1>(a, W, nbx, batch, st);
+      case COL_ETD_2: return col_m<COL_ETD_2>(a, W, nbx, batch, st);
+      case COL_ETD_3: return col_m<COL_ETD_3>(a, W, nbx, batch, st);
+      case COL_ETD_4: return col_m<COL_ETD_4>(a, W, nbx, batch, st);
+      default: return cudaErrorInvalidValue;
+    }
+  }
   static cudaError_t row(const RowArgs<T>& a, int P, int nby, int batch, cudaStream_t st) {
-    if (P * (N / FFT_E) > max_threads(row_pass_kernel<T, N>)) return cudaErrorInvalidConfiguration;
+    if (P * pass_tpl<T, N>() > max_threads(row_pass_kernel<T, N>)) return cudaErrorInvalidConfiguration;
     const size_t smem = (size_t)P * line_bytes();
     cudaError_t e = cudaFuncSetAttribute(row_pass_kernel<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    row_pass_kernel<T, N><<<dim3(nby, batch), dim3(P * (N / FFT_E)), smem, st>>>(a);
+    row_pass_kernel<T, N><<<dim3(nby, batch), dim3(P * pass_tpl<T, N>()), smem, st>>>(a);
     return cudaGetLastError();
   }
 };
 
-#define PTF_FOR_SIZES(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
-
-template <typename T>
-cudaError_t launch_col2d_impl(int ny, const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st) {
-  switch (ny) {
-#define PTF_CASE(n) case n: return PassLaunch<T, n>::col(a, W, nbx, batch, st);
-    PTF_FOR_SIZES(PTF_CASE)
-#undef PTF_CASE
-    default: return cudaErrorInvalidValue;
-  }
-}
-template <typename T>
-cudaError_t launch_row2d_impl(int nx, const RowArgs<T>& a, int P, int nby, int batch, cudaStream_t st) {
-  switch (nx) {
-#define PTF_CASE(n) case n: return PassLaunch<T, n>::row(a, P, nby, batch, st);
-    PTF_FOR_SIZES(PTF_CASE)
-#undef PTF_CASE
-    default: return cudaErrorInvalidValue;
-  }
-}
 template <typename T, int N> int max_lines_n(bool col) {
   typedef typename cplx_of<T>::type C;
-  const size_t lb = (size_t)line_stride(N) * sizeof(C);
-  int m = (int)((160u * 1024u) / lb);
-  const int tpl = N / FFT_E;
-  const int mt = col ? PassLaunch<T, N>::max_threads(col_pass_kernel<T, N>)
+  const size_t lb = col ? col_smem_bytes<T, N>(1) : (size_t)line_stride(N) * sizeof(C);
+  int m = (int)((200u * 1024u) / lb);
+  const int tpl = pass_tpl<T, N>();
+  // the ETDRK4 stage-1 kernel carries the most state: it bounds every mode
+  const int mt = col ? PassLaunch<T, N>::max_threads(col_pass_kernel<T, N, COL_ETD_1>)
                      : PassLaunch<T, N>::max_threads(row_pass_kernel<T, N>);
   while (m > 1 && m * tpl > mt) --m;
   return m < 1 ? 1 : m;
 }
-// Largest number of lines (columns W or row pairs P) per block for length n.
-template <typename T> int max_lines_impl(int n, bool col) {
-  switch (n) {
-#define PTF_CASE(v) case v: return max_lines_n<T, v>(col);
-    PTF_FOR_SIZES(PTF_CASE)
-#undef PTF_CASE
-    default: return 1;
-  }
-}
+
+#define PTF_FOR_SIZES(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
 
 }  // namespace ptf
-
-#define PTF_INSTANTIATE_2D(T)                                                                            \
-  namespace ptf {                                                                                        \
-  template <> cudaError_t launch_col2d<T>(int ny, const ColArgs<T>& a, int W, int nbx, int batch,       \
-                                          cudaStream_t st) {                                             \
-    return launch_col2d_impl<T>(ny, a, W, nbx, batch, st);                                               \
-  }                                                                                                      \
-  template <> cudaError_t launch_row2d<T>(int nx, const RowArgs<T>& a, int P, int nby, int batch,       \
-                                          cudaStream_t st) {                                             \
-    return launch_row2d_impl<T>(nx, a, P, nby, batch, st);                                               \
-  }                                                                                                      \
-  template <> int max_lines_per_block<T>(int n, bool col) { return max_lines_impl<T>(n, col); }                         \
-  }

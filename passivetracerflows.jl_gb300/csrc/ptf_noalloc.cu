@@ -134,18 +134,8 @@ int ptf_calcN2d_noalloc(int32_t nx, int32_t ny, double Lx, double Ly, const doub
   if (e == cudaSuccess) e = launch_real_in<double>(v, V, (long long)nx * ny, -1.0 / (2.0 * nx * ny), st);
   if (e != cudaSuccess) return fail(PTF_ERR_CUDA, std::string("input conversion: ") + cudaGetErrorString(e));
 
-  int W = 2;
-  const int wmax = max_lines_per_block<double>(ny, true);
-  while (W * (ny / 16) < 64 && W < 8) W *= 2;
-  if (W > wmax) W = wmax;
-  while (pitch % W) W /= 2;
-  if (W < 1) W = 1;
-  int P = 1;
-  const int pmax = max_lines_per_block<double>(nx, false);
-  while (P * (nx / 16) < 64 && P < 16) P *= 2;
-  if (P > pmax) P = pmax;
-  while ((ny / 2) % P) P /= 2;
-  if (P < 1) P = 1;
+  const int W = default_lines_per_block<double>(ny, true, pitch);
+  const int P = default_lines_per_block<double>(nx, false, ny / 2);
 
   ColArgs<double> ca;
   std::memset(&ca, 0, sizeof(ca));

@@ -24,7 +24,7 @@ namespace ptf {
 enum ColMode : int {
   COL_PROLOGUE = 0,   // s -> A, B
   COL_FWD_STORE = 1,  // s = Fy(Nx) ; then A, B of s
-  COL_RK4_1 = 2, COL_RK4_2 = 3, COL_RK4_3 = 4, COL_RK4_4 = 5,
+  COL_RK4_1 = 2, COL_RK4_2 = 3, COL_RK4_3 = 4, COL_RK4_4 = 5,   // RK4 stages
   COL_ETD_1 = 6, COL_ETD_2 = 7, COL_ETD_3 = 8, COL_ETD_4 = 9,
   COL_FWD_N = 10,     // nout = Fy(Nx), nothing else (calcN)
 };
@@ -70,135 +70,168 @@ __device__ __forceinline__ T lval(int p, T dky) { return (T)(p < NY / 2 ? p : p 
 // ---------------------------------------------------------------------------
 // Column pass.  blockDim.x = W * (NY/16); w = tid % W selects the column
 // (kr = blockIdx.x*W + w), t = tid / W the thread within the column's line.
+// Consecutive threads therefore touch consecutive kr of one row: a warp
+// reads W-element row segments.  MODE is a compile-time ColMode.
 // ---------------------------------------------------------------------------
-template <typename T, int NY>
-__global__ void col_pass_kernel(ColArgs<T> a) {
+#ifndef PTF_COL_MINB_F32
+#define PTF_COL_MINB_F32 2
+#endif
+#ifndef PTF_COL_MINB_F64
+#define PTF_COL_MINB_F64 1
+#endif
+template <typename T> struct ColBounds { static constexpr int threads = 256, blocks = PTF_COL_MINB_F64; };
+template <> struct ColBounds<float> { static constexpr int threads = 256, blocks = PTF_COL_MINB_F32; };
+// Dynamic shared memory of a column-pass block with W lines: the W FFT
+// lines, then a private slot array holding each thread's 16 stage outputs
+// between the two inverse transforms.
+template <typename T, int NY> __host__ __device__ constexpr size_t col_smem_bytes(int W) {
+  return (size_t)W * (line_stride(NY) + NY) * sizeof(typename cplx_of<T>::type);
+}
+template <typename T, int N> __host__ __device__ constexpr int pass_tpl() { return N / PassE<T, N>::value;
+}
+
+template <typename T, int NY, int MODE>
+__global__ void __launch_bounds__(ColBounds<T>::threads, ColBounds<T>::blocks) col_pass_kernel(ColArgs<T> a) {
   typedef typename cplx_of<T>::type C;
-  constexpr int E = FFT_E;
+  constexpr int E = PassE<T, NY>::value;
+  constexpr int TPL = NY / E;
   constexpr int LS = line_stride(NY);
-  constexpr int RF = LastRadix<NY, -1>::value;   // forward output pattern
-  constexpr int RI = FirstRadix<NY, +1>::value;  // inverse input pattern (== RF)
-  constexpr int RO = LastRadix<NY, +1>::value;   // inverse output pattern
+  constexpr int RF0 = FirstRadix<NY, -1, E>::value;  // forward input pattern
+  constexpr int RF = LastRadix<NY, -1, E>::value;    // forward output pattern
+  constexpr int RI = FirstRadix<NY, +1, E>::value;   // inverse input pattern (== RF)
+  constexpr int RO = LastRadix<NY, +1, E>::value;    // inverse output pattern
   static_assert(RF == RI, "forward-last and inverse-first radices must match");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* sm = reinterpret_cast<C*>(smem_raw);
-  const int W = blockDim.x / (NY / E);
+  const int W = blockDim.x / TPL;
   const int w = threadIdx.x % W, t = threadIdx.x / W;
   const int kr = blockIdx.x * W + w;
-  const long long boff = (long long)blockIdx.y * a.bstride;
-  const long long plane = (long long)NY * a.pitch;
-  const long long toff = a.tab_per_solve ? (long long)blockIdx.y * plane : 0;
   const int pitch = a.pitch;
+  const size_t boff = (size_t)blockIdx.y * (size_t)a.bstride;
+  const size_t plane = (size_t)NY * (size_t)pitch;
+  const size_t toff = a.tab_per_solve ? (size_t)blockIdx.y * plane : 0;
   C* line = sm + w * LS;
-  const int mode = a.mode;
+  const int tb = t * pitch + kr;  // this thread's offset inside one field
+  // offset of register i for a first/last stage of radix R
+#define PTF_OFF(R, i) (tb + (((i) / (R)) * TPL + ((i) % (R)) * (NY / (R))) * pitch)
 
   C v[E];
-  if (mode != COL_PROLOGUE) {
-    constexpr int R0 = FirstRadix<NY, -1>::value;
+  if (MODE != COL_PROLOGUE) {
+    const C* __restrict__ src = a.nxin + boff;
 #pragma unroll
-    for (int i = 0; i < E; ++i) v[i] = a.nxin[boff + (long long)reg_pos<NY, R0>(t, i) * pitch + kr];
-    fft_line<NY, -1>(v, t, line, a.tw);
+    for (int i = 0; i < E; ++i) v[i] = src[PTF_OFF(RF0, i)];
+    fft_line<NY, -1, E>(v, t, line, a.tw);
   }
 
-  // Stage combination at the positions p = reg_pos<NY, RF>(t, i).
+  // Stage combination at the positions p = reg_pos<NY, RF, E>(t, i).  The next
+  // stage input is parked in this thread's slots of `park` (slot i at
+  // park[i*blockDim + tid]: conflict-free, no barrier needed since each
+  // thread reads back only what it wrote).
   const T dt = a.dt;
-  C sn[E];
+  C* park = sm + W * LS;
+  const int nthr = blockDim.x;
+  {
+    C* __restrict__ S = a.s + boff;
+    C* __restrict__ SI = a.si + boff;
+    C* __restrict__ AC = a.acc + boff;
+    C* __restrict__ N1p = a.n1 + boff;
+    const T* __restrict__ Lt = a.Ltab + toff;
+    const T* __restrict__ cf = a.coef + 6 * toff;
 #pragma unroll
-  for (int i = 0; i < E; ++i) {
-    const int p = reg_pos<NY, RF>(t, i);
-    const long long o = boff + (long long)p * pitch + kr;
-    const long long to = toff + (long long)p * pitch + kr;       // L table
-    const long long co = 6 * toff + (long long)p * pitch + kr;   // ETDRK4 tables
-    const C N = v[i];
-    C x;
-    switch (mode) {
-      case COL_PROLOGUE: x = a.s[o]; break;
-      case COL_FWD_STORE: x = N; a.s[o] = x; break;
-      case COL_FWD_N: x = N; a.nout[o] = N; break;
-      case COL_RK4_1: {
-        const T L = a.Ltab[to];
-        const C s = a.s[o];
+    for (int i = 0; i < E; ++i) {
+      const int o = PTF_OFF(RF, i);
+      const C N = v[i];
+      C x;
+      if (MODE == COL_PROLOGUE) {
+        x = S[o];
+      } else if (MODE == COL_FWD_STORE) {
+        x = N; S[o] = x;
+      } else if (MODE == COL_FWD_N) {
+        x = N; a.nout[boff + o] = N;
+      } else if (MODE == COL_RK4_1) {
+        const T L = Lt[o];
+        const C s = S[o];
         C k; k.x = L * s.x + N.x; k.y = L * s.y + N.y;
         C ac; ac.x = s.x + (dt / 6) * k.x; ac.y = s.y + (dt / 6) * k.y;
-        a.acc[o] = ac;
+        AC[o] = ac;
         x.x = s.x + (dt / 2) * k.x; x.y = s.y + (dt / 2) * k.y;
-        a.si[o] = x;
-      } break;
-      case COL_RK4_2:
-      case COL_RK4_3: {
-        const T L = a.Ltab[to];
-        const C si = a.si[o], s = a.s[o];
+        SI[o] = x;
+      } else if (MODE == COL_RK4_2 || MODE == COL_RK4_3) {
+        const T L = Lt[o];
+        const C si = SI[o], s = S[o];
+        C ac = AC[o];
         C k; k.x = L * si.x + N.x; k.y = L * si.y + N.y;
-        C ac = a.acc[o];
         ac.x += (dt / 3) * k.x; ac.y += (dt / 3) * k.y;
-        a.acc[o] = ac;
-        const T h = (mode == COL_RK4_2) ? dt / 2 : dt;
+        AC[o] = ac;
+        const T h = (MODE == COL_RK4_2) ? dt / 2 : dt;
         x.x = s.x + h * k.x; x.y = s.y + h * k.y;
-        a.si[o] = x;
-      } break;
-      case COL_RK4_4: {
-        const T L = a.Ltab[to];
-        const C si = a.si[o];
+        SI[o] = x;
+      } else if (MODE == COL_RK4_4) {
+        const T L = Lt[o];
+        const C si = SI[o], ac = AC[o];
         C k; k.x = L * si.x + N.x; k.y = L * si.y + N.y;
-        const C ac = a.acc[o];
         x.x = ac.x + (dt / 6) * k.x; x.y = ac.y + (dt / 6) * k.y;
-        a.s[o] = x;
-      } break;
-      case COL_ETD_1: {
-        const T* cf = a.coef + co;
-        const T Ee = cf[0], E2 = cf[plane], ze = cf[2 * plane], al = cf[3 * plane];
-        const C s = a.s[o];
-        a.n1[o] = N;
+        S[o] = x;
+      } else if (MODE == COL_ETD_1) {
+        const T Ee = cf[o], E2 = cf[o + plane], ze = cf[o + 2 * plane], al = cf[o + 3 * plane];
+        const C s = S[o];
+        N1p[o] = N;
         C ac; ac.x = Ee * s.x + al * N.x; ac.y = Ee * s.y + al * N.y;
-        a.acc[o] = ac;
+        AC[o] = ac;
         x.x = E2 * s.x + ze * N.x; x.y = E2 * s.y + ze * N.y;
-        a.si[o] = x;
-      } break;
-      case COL_ETD_2: {
-        const T* cf = a.coef + co;
-        const T E2 = cf[plane], ze = cf[2 * plane], be = cf[4 * plane];
-        const C s = a.s[o];
-        C ac = a.acc[o];
+        SI[o] = x;
+      } else if (MODE == COL_ETD_2) {
+        const T E2 = cf[o + plane], ze = cf[o + 2 * plane], be = cf[o + 4 * plane];
+        const C s = S[o];
+        C ac = AC[o];
         ac.x += 2 * be * N.x; ac.y += 2 * be * N.y;
-        a.acc[o] = ac;
+        AC[o] = ac;
         x.x = E2 * s.x + ze * N.x; x.y = E2 * s.y + ze * N.y;
-      } break;
-      case COL_ETD_3: {
-        const T* cf = a.coef + co;
-        const T E2 = cf[plane], ze = cf[2 * plane], be = cf[4 * plane];
-        const C s1 = a.si[o], N1 = a.n1[o];
-        C ac = a.acc[o];
+      } else if (MODE == COL_ETD_3) {
+        const T E2 = cf[o + plane], ze = cf[o + 2 * plane], be = cf[o + 4 * plane];
+        const C s1 = SI[o], N1 = N1p[o];
+        C ac = AC[o];
         ac.x += 2 * be * N.x; ac.y += 2 * be * N.y;
-        a.acc[o] = ac;
+        AC[o] = ac;
         x.x = E2 * s1.x + ze * (2 * N.x - N1.x); x.y = E2 * s1.y + ze * (2 * N.y - N1.y);
-      } break;
-      default: {  // COL_ETD_4
-        const T ga = a.coef[co + 5 * plane];
-        const C ac = a.acc[o];
+      } else {  // COL_ETD_4
+        const T ga = cf[o + 5 * plane];
+        const C ac = AC[o];
         x.x = ac.x + ga * N.x; x.y = ac.y + ga * N.y;
-        a.s[o] = x;
-      } break;
+        S[o] = x;
+      }
+      park[i * nthr + threadIdx.x] = x;
     }
-    sn[i] = x;
   }
-  if (!a.do_inverse) return;  // uniform across the block
+  if (MODE == COL_FWD_N || !a.do_inverse) return;  // uniform across the block
 
   // A = Fy^-1(s_next)
 #pragma unroll
-  for (int i = 0; i < E; ++i) v[i] = sn[i];
-  fft_line<NY, +1>(v, t, line, a.tw);
+  for (int i = 0; i < E; ++i) v[i] = park[i * nthr + threadIdx.x];
+  fft_line<NY, +1, E>(v, t, line, a.tw);
+  {
+    C* __restrict__ Ap = a.A + boff;
 #pragma unroll
-  for (int i = 0; i < E; ++i) a.A[boff + (long long)reg_pos<NY, RO>(t, i) * pitch + kr] = v[i];
+    for (int i = 0; i < E; ++i) Ap[PTF_OFF(RO, i)] = v[i];
+  }
+  // Keep the second transform from being interleaved with the first (that
+  // doubles the live registers): memory operations cannot cross this.
+  asm volatile("" ::: "memory");
   // B = Fy^-1(i l s_next)
 #pragma unroll
   for (int i = 0; i < E; ++i) {
-    const T l = lval<T, NY>(reg_pos<NY, RI>(t, i), a.dky);
-    v[i].x = -l * sn[i].y;
-    v[i].y = l * sn[i].x;
+    const T l = lval<T, NY>(reg_pos<NY, RI, E>(t, i), a.dky);
+    const C x = park[i * nthr + threadIdx.x];
+    v[i].x = -l * x.y;
+    v[i].y = l * x.x;
   }
-  fft_line<NY, +1>(v, t, line, a.tw);
+  fft_line<NY, +1, E>(v, t, line, a.tw);
+  {
+    C* __restrict__ Bp = a.B + boff;
 #pragma unroll
-  for (int i = 0; i < E; ++i) a.B[boff + (long long)reg_pos<NY, RO>(t, i) * pitch + kr] = v[i];
+    for (int i = 0; i < E; ++i) Bp[PTF_OFF(RO, i)] = v[i];
+  }
+#undef PTF_OFF
 }
 
 // ---------------------------------------------------------------------------
@@ -252,15 +285,15 @@ __device__ __forceinline__ C zsrc_c2r(const C* A0, const C* A1, int k, int NX) {
 }
 
 template <typename T, int NX>
-__global__ void row_pass_kernel(RowArgs<T> a) {
+__global__ void __launch_bounds__(256) row_pass_kernel(RowArgs<T> a) {
   typedef typename cplx_of<T>::type C;
-  constexpr int E = FFT_E;
+  constexpr int E = PassE<T, NX>::value;
   constexpr int TPL = NX / E;
   constexpr int LS = line_stride(NX);
-  constexpr int RI0 = FirstRadix<NX, +1>::value;
-  constexpr int RIL = LastRadix<NX, +1>::value;   // == 16
-  constexpr int RF0 = FirstRadix<NX, -1>::value;  // == 16
-  constexpr int RFL = LastRadix<NX, -1>::value;
+  constexpr int RI0 = FirstRadix<NX, +1, E>::value;
+  constexpr int RIL = LastRadix<NX, +1, E>::value;   // == E
+  constexpr int RF0 = FirstRadix<NX, -1, E>::value;  // == E
+  constexpr int RFL = LastRadix<NX, -1, E>::value;
   static_assert(RIL == RF0, "inverse-last and forward-first radices must match");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* sm = reinterpret_cast<C*>(smem_raw);
@@ -281,18 +314,18 @@ __global__ void row_pass_kernel(RowArgs<T> a) {
   if (a.mode == ROW_R2C) {
 #pragma unroll
     for (int i = 0; i < E; ++i) {
-      const int x = reg_pos<NX, RF0>(t, i);
+      const int x = reg_pos<NX, RF0, E>(t, i);
       v[i].x = a.cin[poff + q0 + x];
       v[i].y = a.cin[poff + q1 + x];
     }
   } else if (a.mode == ROW_C2R) {
 #pragma unroll
-    for (int i = 0; i < E; ++i) v[i] = zsrc_c2r<C>(a.A + r0, a.A + r1, reg_pos<NX, RI0>(t, i), NX);
-    fft_line<NX, +1>(v, t, line, a.tw);
+    for (int i = 0; i < E; ++i) v[i] = zsrc_c2r<C>(a.A + r0, a.A + r1, reg_pos<NX, RI0, E>(t, i), NX);
+    fft_line<NX, +1, E>(v, t, line, a.tw);
     if (valid) {
 #pragma unroll
       for (int i = 0; i < E; ++i) {
-        const int x = reg_pos<NX, RIL>(t, i);
+        const int x = reg_pos<NX, RIL, E>(t, i);
         a.cout[poff + q0 + x] = v[i].x * a.scale;
         a.cout[poff + q1 + x] = v[i].y * a.scale;
       }
@@ -301,16 +334,16 @@ __global__ void row_pass_kernel(RowArgs<T> a) {
   } else {  // ROW_RHS
     C z0[E];
 #pragma unroll
-    for (int i = 0; i < E; ++i) v[i] = zsrc_rhs<T, C>(a.A + r0, a.B + r0, reg_pos<NX, RI0>(t, i), NX, a.dkx);
-    fft_line<NX, +1>(v, t, line, a.tw);
+    for (int i = 0; i < E; ++i) v[i] = zsrc_rhs<T, C>(a.A + r0, a.B + r0, reg_pos<NX, RI0, E>(t, i), NX, a.dkx);
+    fft_line<NX, +1, E>(v, t, line, a.tw);
 #pragma unroll
     for (int i = 0; i < E; ++i) z0[i] = v[i];
 #pragma unroll
-    for (int i = 0; i < E; ++i) v[i] = zsrc_rhs<T, C>(a.A + r1, a.B + r1, reg_pos<NX, RI0>(t, i), NX, a.dkx);
-    fft_line<NX, +1>(v, t, line, a.tw);
+    for (int i = 0; i < E; ++i) v[i] = zsrc_rhs<T, C>(a.A + r1, a.B + r1, reg_pos<NX, RI0, E>(t, i), NX, a.dkx);
+    fft_line<NX, +1, E>(v, t, line, a.tw);
 #pragma unroll
     for (int i = 0; i < E; ++i) {
-      const int x = reg_pos<NX, RIL>(t, i);
+      const int x = reg_pos<NX, RIL, E>(t, i);
       const T u0 = a.u[foff + q0 + x], v0 = a.v[foff + q0 + x];
       const T u1 = a.u[foff + q1 + x], v1 = a.v[foff + q1 + x];
       C w;
@@ -320,10 +353,10 @@ __global__ void row_pass_kernel(RowArgs<T> a) {
     }
   }
   // forward x-FFT of n_y0 + i n_y1
-  fft_line<NX, -1>(v, t, line, a.tw);
+  fft_line<NX, -1, E>(v, t, line, a.tw);
   __syncthreads();
 #pragma unroll
-  for (int i = 0; i < E; ++i) line[smem_pad(reg_pos<NX, RFL>(t, i))] = v[i];
+  for (int i = 0; i < E; ++i) line[smem_pad(reg_pos<NX, RFL, E>(t, i))] = v[i];
   __syncthreads();
   const T sc = a.scale;
   if (valid) {
