@@ -345,15 +345,18 @@ def stepforward(prob: Problem, nsteps: int = 1):
         prob.clock.step += 1
 
 
+def _as_num(a):
+    a = np.asarray(a)
+    return a.astype(np.complex128) if np.iscomplexobj(a) else a.astype(np.float64)
+
+
 def rel_l2(a, b):
-    """‖a-b‖₂ / ‖b‖₂."""
-    a = np.asarray(a, dtype=np.float64)
-    b = np.asarray(b, dtype=np.float64)
+    """‖a-b‖₂ / ‖b‖₂ (real or complex arrays)."""
+    a, b = _as_num(a), _as_num(b)
     return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
 
 
 def isapprox(a, b, rtol):
     """Julia ``isapprox`` on arrays: ‖a-b‖ ≤ rtol·max(‖a‖, ‖b‖)."""
-    a = np.asarray(a, dtype=np.float64).ravel()
-    b = np.asarray(b, dtype=np.float64).ravel()
+    a, b = _as_num(a).ravel(), _as_num(b).ravel()
     return bool(np.linalg.norm(a - b) <= rtol * max(np.linalg.norm(a), np.linalg.norm(b)))

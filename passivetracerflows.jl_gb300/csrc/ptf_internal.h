@@ -1,7 +1,7 @@
 // Internal declarations shared by the translation units of libptf.so.
 #pragma once
 #include <cuda_runtime.h>
-#include "ptf_pass2d.cuh"
+#include "ptf_passes.cuh"
 
 #include <string>
 
@@ -10,11 +10,11 @@ namespace ptf {
 // Message returned by ptf_last_error(NULL) (calls without a handle).
 void set_global_error(const std::string& msg);
 
-// Pass launchers (defined in ptf_kern2d_f64.cu / ptf_kern2d_f32.cu).
-// Column pass: grid (nbx, batch), nbx*W columns, W columns per block.
-template <typename T> cudaError_t launch_col2d(int ny, const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st);
-// Row pass: grid (nby, batch), P row pairs per block.
-template <typename T> cudaError_t launch_row2d(int nx, const RowArgs<T>& a, int P, int nby, int batch, cudaStream_t st);
+// Pass launchers (ptf_kern2d.cu dispatching to ptf_k2d_inst.cu objects).
+// Column pass over transform length n: grid (nbx, nby), W columns per block.
+template <typename T> cudaError_t launch_col(int n, const ColArgs<T>& a, int W, int nbx, int nby, cudaStream_t st);
+// Row pass over x length nx: grid (nbx, batch), P row pairs per block.
+template <typename T> cudaError_t launch_row(int nx, const RowArgs<T>& a, int P, int nbx, int batch, cudaStream_t st);
 // Largest W / P that a launch may use for a given length (shared-memory bound).
 template <typename T> int max_lines_per_block(int n, bool col);
 // Default W (col) or P (row) for length n; `divisor` must be divisible by it.

@@ -14,8 +14,8 @@ PTF_FOR_SIZES(PTF_EXTERN)
 #undef PTF_EXTERN
 
 template <typename T>
-cudaError_t launch_col2d(int ny, const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st) {
-  switch (ny) {
+cudaError_t launch_col(int n, const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st) {
+  switch (n) {
 #define PTF_CASE(n) case n: return PassLaunch<T, n>::col(a, W, nbx, batch, st);
     PTF_FOR_SIZES(PTF_CASE)
 #undef PTF_CASE
@@ -23,7 +23,7 @@ cudaError_t launch_col2d(int ny, const ColArgs<T>& a, int W, int nbx, int batch,
   }
 }
 template <typename T>
-cudaError_t launch_row2d(int nx, const RowArgs<T>& a, int P, int nby, int batch, cudaStream_t st) {
+cudaError_t launch_row(int nx, const RowArgs<T>& a, int P, int nby, int batch, cudaStream_t st) {
   switch (nx) {
 #define PTF_CASE(n) case n: return PassLaunch<T, n>::row(a, P, nby, batch, st);
     PTF_FOR_SIZES(PTF_CASE)
@@ -68,10 +68,10 @@ template <typename T> int default_lines_per_block(int n, bool col, int divisor) 
   return m < 1 ? 1 : m;
 }
 
-template cudaError_t launch_col2d<float>(int, const ColArgs<float>&, int, int, int, cudaStream_t);
-template cudaError_t launch_col2d<double>(int, const ColArgs<double>&, int, int, int, cudaStream_t);
-template cudaError_t launch_row2d<float>(int, const RowArgs<float>&, int, int, int, cudaStream_t);
-template cudaError_t launch_row2d<double>(int, const RowArgs<double>&, int, int, int, cudaStream_t);
+template cudaError_t launch_col<float>(int, const ColArgs<float>&, int, int, int, cudaStream_t);
+template cudaError_t launch_col<double>(int, const ColArgs<double>&, int, int, int, cudaStream_t);
+template cudaError_t launch_row<float>(int, const RowArgs<float>&, int, int, int, cudaStream_t);
+template cudaError_t launch_row<double>(int, const RowArgs<double>&, int, int, int, cudaStream_t);
 template int max_lines_per_block<float>(int, bool);
 template int max_lines_per_block<double>(int, bool);
 template int default_lines_per_block<float>(int, bool, int);

@@ -36,12 +36,13 @@ template <typename T, int N> struct PassLaunch {
       case COL_ETD_2: return col_m<COL_ETD_2>(a, W, nbx, batch, st);
       case COL_ETD_3: return col_m<COL_ETD_3>(a, W, nbx, batch, st);
       case COL_ETD_4: return col_m<COL_ETD_4>(a, W, nbx, batch, st);
+      case COL_YINV3: return col_m<COL_YINV3>(a, W, nbx, batch, st);
       default: return cudaErrorInvalidValue;
     }
   }
   static cudaError_t row(const RowArgs<T>& a, int P, int nby, int batch, cudaStream_t st) {
     if (P * pass_tpl<T, N>() > max_threads(row_pass_kernel<T, N>)) return cudaErrorInvalidConfiguration;
-    const size_t smem = (size_t)P * line_bytes();
+    const size_t smem = row_smem_bytes<T, N>(P);
     cudaError_t e = cudaFuncSetAttribute(row_pass_kernel<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     row_pass_kernel<T, N><<<dim3(nby, batch), dim3(P * pass_tpl<T, N>()), smem, st>>>(a);
@@ -51,7 +52,8 @@ template <typename T, int N> struct PassLaunch {
 
 template <typename T, int N> int max_lines_n(bool col) {
   typedef typename cplx_of<T>::type C;
-  const size_t lb = col ? col_smem_bytes<T, N>(1) : (size_t)line_stride(N) * sizeof(C);
+  const size_t lb = col ? col_smem_bytes<T, N>(1) : row_smem_bytes<T, N>(1);
+  (void)sizeof(C);
   int m = (int)((200u * 1024u) / lb);
   const int tpl = pass_tpl<T, N>();
   // the ETDRK4 stage-1 kernel carries the most state: it bounds every mode

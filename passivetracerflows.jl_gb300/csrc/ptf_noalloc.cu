@@ -140,23 +140,25 @@ int ptf_calcN2d_noalloc(int32_t nx, int32_t ny, double Lx, double Ly, const doub
   ColArgs<double> ca;
   std::memset(&ca, 0, sizeof(ca));
   ca.s = S; ca.A = A; ca.B = B; ca.tw = twy;
-  ca.dky = 2 * M_PI / Ly;
-  ca.pitch = pitch; ca.mode = COL_PROLOGUE; ca.do_inverse = 1;
-  e = launch_col2d<double>(ny, ca, W, pitch / W, 1, st);
+  ca.dk = 2 * M_PI / Ly;
+  ca.stride = pitch; ca.mode = COL_PROLOGUE; ca.do_inverse = 1;
+  ca.tplane = (long long)ny * pitch;
+  e = launch_col<double>(ny, ca, W, pitch / W, 1, st);
   if (e != cudaSuccess) return fail(PTF_ERR_CUDA, std::string("column pass: ") + cudaGetErrorString(e));
   RowArgs<double> ra;
   std::memset(&ra, 0, sizeof(ra));
   ra.A = A; ra.B = B; ra.out = NX; ra.u = U; ra.v = V; ra.tw = twx;
   ra.dkx = 2 * M_PI / Lx; ra.scale = 1.0;
-  ra.ny = ny; ra.pitch = pitch; ra.mode = ROW_RHS;
-  e = launch_row2d<double>(nx, ra, P, (ny / 2) / P, 1, st);
+  ra.rows = ny; ra.pitch = pitch; ra.mode = ROW_RHS;
+  e = launch_row<double>(nx, ra, P, (ny / 2) / P, 1, st);
   if (e != cudaSuccess) return fail(PTF_ERR_CUDA, std::string("row pass: ") + cudaGetErrorString(e));
   ColArgs<double> cf;
   std::memset(&cf, 0, sizeof(cf));
   cf.nxin = NX; cf.nout = S; cf.tw = twy;
-  cf.dky = 2 * M_PI / Ly;
-  cf.pitch = pitch; cf.mode = COL_FWD_N; cf.do_inverse = 0;
-  e = launch_col2d<double>(ny, cf, W, pitch / W, 1, st);
+  cf.dk = 2 * M_PI / Ly;
+  cf.stride = pitch; cf.mode = COL_FWD_N; cf.do_inverse = 0;
+  cf.tplane = (long long)ny * pitch;
+  e = launch_col<double>(ny, cf, W, pitch / W, 1, st);
   if (e != cudaSuccess) return fail(PTF_ERR_CUDA, std::string("column pass: ") + cudaGetErrorString(e));
   e = launch_spec_out<double>(S, (double2*)N, nkr, pitch, ny, st);
   if (e != cudaSuccess) return fail(PTF_ERR_CUDA, std::string("output conversion: ") + cudaGetErrorString(e));

@@ -59,7 +59,27 @@ def cellular128_etdrk4():
     return dict(c50=p.vars.c.copy(), t=p.clock.t, step=p.clock.step)
 
 
-FIXTURES = {"cellular128_rk4": cellular128_rk4, "cellular128_etdrk4": cellular128_etdrk4}
+def abc_flow(A=1.0, B=np.sqrt(2 / 3), C=np.sqrt(1 / 3)):
+    """ABC flow: u = A sin z + C cos y, v = B sin x + A cos z, w = C sin y + B cos x."""
+    u = lambda x, y, z: A * np.sin(z) + C * np.cos(y)
+    v = lambda x, y, z: B * np.sin(x) + A * np.cos(z)
+    w = lambda x, y, z: C * np.sin(y) + B * np.cos(x)
+    return u, v, w
+
+
+def abc32_etdrk4():
+    """3D ABC flow, 32³, κ=η=ι=5e-4, Gaussian σ=0.3 at the domain centre, ETDRK4, dt=0.005; c at step 100."""
+    u, v, w = abc_flow()
+    p = o.Problem(o.ThreeDAdvectingFlow(u=u, v=v, w=w), nx=32, Lx=2 * np.pi, kappa=5e-4, dt=0.005, stepper="ETDRK4")
+    x, y, z = p.grid.gridpoints()
+    c0 = np.exp(-(x ** 2 + y ** 2 + z ** 2) / (2 * 0.3 ** 2))
+    o.set_c(p, c0)
+    o.stepforward(p, 100); o.updatevars(p)
+    return dict(c0=c0, c100=p.vars.c.copy(), t=p.clock.t, step=p.clock.step)
+
+
+FIXTURES = {"cellular128_rk4": cellular128_rk4, "cellular128_etdrk4": cellular128_etdrk4,
+            "abc32_etdrk4": abc32_etdrk4}
 
 if __name__ == "__main__":
     names = sys.argv[1:] or list(FIXTURES)

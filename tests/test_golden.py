@@ -33,3 +33,11 @@ def test_golden_mass_conservation(oracle):
     g = np.load(GOLD / "cellular128_rk4.npz")
     m0, m1 = g["c0"].sum(), g["c2000"].sum()
     assert abs(m1 - m0) / abs(m0) < 1e-12
+
+
+def test_golden_abc32_etdrk4(oracle):
+    g = np.load(GOLD / "abc32_etdrk4.npz")
+    d = _mod().abc32_etdrk4()
+    assert oracle.rel_l2(d["c100"], g["c100"]) <= 1e-13
+    m0, m1 = g["c0"].sum(), g["c100"].sum()
+    assert abs(m1 - m0) / abs(m0) < 1e-10

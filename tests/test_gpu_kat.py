@@ -20,3 +20,15 @@ def test_reference_kat_2d_gpu(gpu, name, tight, stepper):
 def test_diffusion2D_timevarying_gpu(gpu):
     err, rtol = kat.diffusion2D(gpu, gpu.GPU(), steadyflow=False)
     assert err <= rtol and err <= 1e-9
+
+
+@pytest.mark.parametrize("name,tight", [("constvel3D", 2e-8), ("timedependentvel3D", 1e-10)])
+def test_reference_kat_3d_gpu(gpu, name, tight):
+    err, rtol = getattr(kat, name)(gpu, gpu.GPU(), n=128)  # the reference's 128³
+    assert err <= rtol and err <= tight
+
+
+@pytest.mark.parametrize("steadyflow", [True, False])
+def test_reference_kat_diffusion3D_gpu(gpu, steadyflow):
+    err, rtol = kat.diffusion3D(gpu, gpu.GPU(), steadyflow=steadyflow)
+    assert err <= rtol and err <= 4.1e-4
