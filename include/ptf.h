@@ -127,6 +127,104 @@ int ptf_profile_read(ptf_handle* h, int32_t kind, double* total_ms, int64_t* lau
 int ptf_kernel_launches(const ptf_handle* h, int64_t* count);
 int32_t ptf_abi_version(void);
 
+/* ---------------------------------------------------------------------------
+ * Batched form.  No single reference counterpart: the reference runs one
+ * Problem at a time; this steps many independent TracerAdvectionDiffusion
+ * problems (each with its own grid size, diffusivity, dt, clock, step count
+ * and flow) together.  Square 2D grids n in {64, 128, 256, 512, 1024}, RK4
+ * (FourierFlows RK4 on the same L and calcN! as ptf_step).  Each stage of
+ * all solves is one persistent kernel launch; a step is replayed from a
+ * captured CUDA graph.
+ * ------------------------------------------------------------------------- */
+enum ptf_flow_kind {
+  PTF_FLOW_ARRAYS = 0,   /* steady flow given as grid arrays u, v */
+  PTF_FLOW_CELLULAR = 1  /* psi = U cos(Kx x + eps sin(omega t)) cos(Ky y), u = -dpsi/dy, v = dpsi/dx,
+                            evaluated on the device at clock.t (PTF_CLOCK_T) or at stage times */
+};
+
+typedef struct ptf_solve_desc {
+  int32_t dim;       /* 2 (batched) or 3 (served through a single-solve handle) */
+  int32_t n;         /* grid points per axis (square / cubic grid) */
+  double L;          /* domain length per axis */
+  double kappa, eta; /* x and y (and z) diffusivities */
+  double kappah;
+  int32_t nkappah;
+  double dt;
+  int64_t nsteps;    /* steps this solve takes */
+  int32_t flow_kind; /* ptf_flow_kind */
+  int32_t time_mode; /* ptf_time_mode (PTF_FLOW_CELLULAR) */
+  double U, eps, omega;
+  int32_t Kx, Ky;    /* integer wavenumbers of the cellular flow (in units of 2 pi / L) */
+} ptf_solve_desc;
+
+typedef struct ptf_batch_config {
+  int32_t precision;        /* ptf_precision */
+  int64_t memory_budget;    /* device bytes the batch may hold (0: unlimited) */
+  int32_t slots_per_bucket; /* solves per same-size bucket (0: about 1 GB of fields per bucket) */
+  int32_t use_graph;        /* replay steps from a captured CUDA graph */
+  int32_t max_slots;        /* total slots over all buckets */
+} ptf_batch_config;
+
+typedef struct ptf_batch ptf_batch;
+
+void ptf_batch_config_default(ptf_batch_config* cfg);
+void ptf_solve_desc_default(ptf_solve_desc* d);
+int ptf_batch_create(const ptf_batch_config* cfg, ptf_batch** out);
+void ptf_batch_destroy(ptf_batch* b);
+const char* ptf_batch_last_error(const ptf_batch* b);
+/* 1 when a solve of this description fits (free slot or budget for a new bucket). */
+int ptf_batch_can_admit(ptf_batch* b, const ptf_solve_desc* d);
+/* set_c! for a new solve (host arrays: c0, and u, v for PTF_FLOW_ARRAYS). */
+int ptf_batch_add(ptf_batch* b, const ptf_solve_desc* d, const double* c0, const double* u, const double* v,
+                  int64_t* id);
+/* stepforward! of every active solve by up to nsteps (each stops at its own nsteps). */
+int ptf_batch_step(ptf_batch* b, int64_t nsteps);
+int ptf_batch_synchronize(ptf_batch* b);
+int ptf_batch_status(ptf_batch* b, int64_t id, int64_t* step, double* t, int32_t* active);
+/* updatevars! + vars.c of one solve (n*n doubles to host). */
+int ptf_batch_get_c(ptf_batch* b, int64_t id, double* c);
+int ptf_batch_remove(ptf_batch* b, int64_t id);
+int ptf_batch_info(ptf_batch* b, int64_t* device_bytes, int64_t* solves, int64_t* kernel_launches);
+int ptf_batch_get_stream(const ptf_batch* b, void** stream);
+
+/* ---------------------------------------------------------------------------
+ * Request server (no reference counterpart): continuous batching.  A worker
+ * thread admits submitted solves by device-memory budget between chunks of
+ * steps, runs everything admitted together, and returns each result when its
+ * own step count is reached.  2D requests run in the batched form, 3D
+ * requests (dim 3, flow arrays) on single-solve handles in the same loop.
+ * ------------------------------------------------------------------------- */
+typedef struct ptf_server_config {
+  int32_t precision;
+  int64_t memory_budget;    /* device bytes for admitted solves (0: unlimited) */
+  int32_t chunk_steps;      /* steps between admission points */
+  int32_t slots_per_bucket;
+} ptf_server_config;
+
+typedef struct ptf_server_stats {
+  int64_t completed, failed, queued, active;
+  double p50_s, p99_s, mean_s;  /* latency from submission to result */
+  double grid_point_steps;      /* sum over completed requests of points x steps */
+  double wall_s;                /* first submission to last completion */
+  int64_t device_bytes;
+} ptf_server_stats;
+
+typedef struct ptf_server ptf_server;
+enum ptf_request_state { PTF_REQ_QUEUED = 0, PTF_REQ_ACTIVE = 1, PTF_REQ_DONE = 2, PTF_REQ_FAILED = 3 };
+
+void ptf_server_config_default(ptf_server_config* cfg);
+int ptf_server_create(const ptf_server_config* cfg, ptf_server** out);
+void ptf_server_destroy(ptf_server* s);
+const char* ptf_server_last_error(const ptf_server* s);
+/* Copies the inputs; w only for 3D.  Returns immediately. */
+int ptf_server_submit(ptf_server* s, const ptf_solve_desc* d, const double* c0, const double* u, const double* v,
+                      const double* w, int64_t* id);
+/* state: ptf_request_state; copies the tracer field into c when done. */
+int ptf_server_poll(ptf_server* s, int64_t id, int32_t* state, double* c);
+int ptf_server_release(ptf_server* s, int64_t id);
+int ptf_server_wait_all(ptf_server* s, double timeout_s);
+int ptf_server_get_stats(ptf_server* s, ptf_server_stats* out);
+
 /* Size of the fixed device scratch used by ptf_calcN2d_noalloc (16 MiB). */
 #define PTF_NOALLOC_SCRATCH_BYTES (16u << 20)
 

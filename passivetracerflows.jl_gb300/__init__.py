@@ -14,7 +14,8 @@ from .traceradvectiondiffusion import (CPU, GPU, Problem, OneDAdvectingFlow, Thr
                                        TwoDAdvectingFlow, ThreeDGrid, TwoDGrid, gridpoints, noflow, set_c,
                                        stepforward, updatevars)
 from ._lib import LIB_PATH, load as load_library
+from .batched import BatchedProblem, Server, SolveSpec
 
 __all__ = ["TracerAdvectionDiffusion", "CPU", "GPU", "Problem", "OneDAdvectingFlow", "TwoDAdvectingFlow",
            "ThreeDAdvectingFlow", "TwoDGrid", "ThreeDGrid", "gridpoints", "noflow", "set_c", "stepforward",
-           "updatevars", "LIB_PATH", "load_library"]
+           "updatevars", "LIB_PATH", "load_library", "BatchedProblem", "Server", "SolveSpec"]

@@ -30,6 +30,37 @@ class PtfConfig(ct.Structure):
     ]
 
 
+PTF_FLOW_ARRAYS, PTF_FLOW_CELLULAR = 0, 1
+PTF_REQ_QUEUED, PTF_REQ_ACTIVE, PTF_REQ_DONE, PTF_REQ_FAILED = 0, 1, 2, 3
+
+
+class PtfSolveDesc(ct.Structure):
+    _fields_ = [
+        ("dim", ct.c_int32), ("n", ct.c_int32), ("L", ct.c_double),
+        ("kappa", ct.c_double), ("eta", ct.c_double), ("kappah", ct.c_double), ("nkappah", ct.c_int32),
+        ("dt", ct.c_double), ("nsteps", ct.c_int64),
+        ("flow_kind", ct.c_int32), ("time_mode", ct.c_int32),
+        ("U", ct.c_double), ("eps", ct.c_double), ("omega", ct.c_double),
+        ("Kx", ct.c_int32), ("Ky", ct.c_int32),
+    ]
+
+
+class PtfBatchConfig(ct.Structure):
+    _fields_ = [("precision", ct.c_int32), ("memory_budget", ct.c_int64), ("slots_per_bucket", ct.c_int32),
+                ("use_graph", ct.c_int32), ("max_slots", ct.c_int32)]
+
+
+class PtfServerConfig(ct.Structure):
+    _fields_ = [("precision", ct.c_int32), ("memory_budget", ct.c_int64), ("chunk_steps", ct.c_int32),
+                ("slots_per_bucket", ct.c_int32)]
+
+
+class PtfServerStats(ct.Structure):
+    _fields_ = [("completed", ct.c_int64), ("failed", ct.c_int64), ("queued", ct.c_int64), ("active", ct.c_int64),
+                ("p50_s", ct.c_double), ("p99_s", ct.c_double), ("mean_s", ct.c_double),
+                ("grid_point_steps", ct.c_double), ("wall_s", ct.c_double), ("device_bytes", ct.c_int64)]
+
+
 class PtfError(RuntimeError):
     """A libptf call returned a non-zero status."""
 
@@ -65,6 +96,33 @@ SIGNATURES = {
     "ptf_kernel_launches": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_int64)]),
     "ptf_calcN2d_noalloc": (ct.c_int, [ct.c_int32, ct.c_int32, ct.c_double, ct.c_double, ct.c_void_p, ct.c_void_p,
                                        ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+    "ptf_batch_config_default": (None, [ct.POINTER(PtfBatchConfig)]),
+    "ptf_solve_desc_default": (None, [ct.POINTER(PtfSolveDesc)]),
+    "ptf_batch_create": (ct.c_int, [ct.POINTER(PtfBatchConfig), ct.POINTER(ct.c_void_p)]),
+    "ptf_batch_destroy": (None, [ct.c_void_p]),
+    "ptf_batch_last_error": (ct.c_char_p, [ct.c_void_p]),
+    "ptf_batch_can_admit": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfSolveDesc)]),
+    "ptf_batch_add": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfSolveDesc), ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                 ct.POINTER(ct.c_int64)]),
+    "ptf_batch_step": (ct.c_int, [ct.c_void_p, ct.c_int64]),
+    "ptf_batch_synchronize": (ct.c_int, [ct.c_void_p]),
+    "ptf_batch_status": (ct.c_int, [ct.c_void_p, ct.c_int64, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_double),
+                                    ct.POINTER(ct.c_int32)]),
+    "ptf_batch_get_c": (ct.c_int, [ct.c_void_p, ct.c_int64, ct.c_void_p]),
+    "ptf_batch_remove": (ct.c_int, [ct.c_void_p, ct.c_int64]),
+    "ptf_batch_info": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_int64),
+                                  ct.POINTER(ct.c_int64)]),
+    "ptf_batch_get_stream": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_void_p)]),
+    "ptf_server_config_default": (None, [ct.POINTER(PtfServerConfig)]),
+    "ptf_server_create": (ct.c_int, [ct.POINTER(PtfServerConfig), ct.POINTER(ct.c_void_p)]),
+    "ptf_server_destroy": (None, [ct.c_void_p]),
+    "ptf_server_last_error": (ct.c_char_p, [ct.c_void_p]),
+    "ptf_server_submit": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfSolveDesc), ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                     ct.c_void_p, ct.POINTER(ct.c_int64)]),
+    "ptf_server_poll": (ct.c_int, [ct.c_void_p, ct.c_int64, ct.POINTER(ct.c_int32), ct.c_void_p]),
+    "ptf_server_release": (ct.c_int, [ct.c_void_p, ct.c_int64]),
+    "ptf_server_wait_all": (ct.c_int, [ct.c_void_p, ct.c_double]),
+    "ptf_server_get_stats": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfServerStats)]),
     "ptf_profile": (ct.c_int, [ct.c_void_p, ct.c_int32]),
     "ptf_profile_read": (ct.c_int, [ct.c_void_p, ct.c_int32, ct.POINTER(ct.c_double), ct.POINTER(ct.c_int64),
                                     ct.POINTER(ct.c_double)]),
@@ -90,10 +148,10 @@ def load(path: os.PathLike | None = None):
     return lib
 
 
-def check(rc: int, handle=None):
+def check(rc: int, handle=None, errfn=None):
     if rc == PTF_OK:
         return
-    msg = load().ptf_last_error(handle)
+    msg = (errfn or load().ptf_last_error)(handle)
     msg = msg.decode() if msg else ""
     if rc == PTF_ERR_ARG:
         raise PtfArgumentError(rc, msg)

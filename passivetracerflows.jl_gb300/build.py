@@ -31,8 +31,12 @@ def _nvcc() -> str:
 
 
 # Per-(precision, length) instantiation units: one source, many objects.
-INST_SOURCES = {"ptf_k2d_inst.cu": [("float", n) for n in (16, 32, 64, 128, 256, 512, 1024, 2048, 4096)]
-                + [("double", n) for n in (16, 32, 64, 128, 256, 512, 1024, 2048, 4096)]}
+_SIZES = (16, 32, 64, 128, 256, 512, 1024, 2048, 4096)
+INST_SOURCES = {
+    "ptf_k2d_inst.cu": [(f"{t}_{n}", [f"-DPTF_T={t}", f"-DPTF_N={n}"]) for t in ("float", "double") for n in _SIZES],
+    "ptf_batch_inst.cu": [(f"{t}_m{m}", [f"-DPTF_T={t}", f"-DPTF_MODE={m}"]) for t in ("float", "double")
+                          for m in (2, 3, 4, 5)],
+}
 
 
 def _units():
@@ -40,8 +44,8 @@ def _units():
     units = []
     for src in sorted(CSRC.glob("*.cu")):
         if src.name in INST_SOURCES:
-            for t, n in INST_SOURCES[src.name]:
-                units.append((src, BUILD / f"{src.stem}_{t}_{n}.o", [f"-DPTF_T={t}", f"-DPTF_N={n}"]))
+            for tag, defs in INST_SOURCES[src.name]:
+                units.append((src, BUILD / f"{src.stem}_{tag}.o", defs))
         else:
             units.append((src, BUILD / (src.stem + ".o"), []))
     return units
@@ -72,7 +76,7 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> Path:
     workers = max(1, min(len(jobs), os.cpu_count() or 1))
     if jobs:
         # the heavy instantiation units first
-        jobs.sort(key=lambda j: (not j[2], -(int(j[2][1].split("=")[1]) if j[2] else 0)))
+        jobs.sort(key=lambda j: (not j[2], "batch" not in j[0].name, -len(str(j[1]))))
         with cf.ThreadPoolExecutor(max_workers=workers) as ex:
             futs = [ex.submit(_compile, nvcc, s, o, list(extra) + d) for s, o, d in jobs]
             for f in futs:

@@ -342,6 +342,7 @@ int run_row(ptf_handle* h, int mode, const void* A, const void* B, const void* C
   a.dkx = (T)(2 * M_PI / h->cfg.Lx);
   a.scale = (T)scale;
   a.rows = (int)h->rows; a.pitch = h->pitch; a.mode = mode;
+  a.park_slots = h->dim == 3 ? 2 : 1;
   a.bstride = h->plane; a.pstride = h->nphys; a.fstride = 0;
   const int P = h->rowP;
   const int nby = (int)((h->rows / 2) / P);

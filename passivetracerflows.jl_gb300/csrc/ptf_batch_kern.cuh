@@ -1,0 +1,117 @@
+// Persistent per-stage kernel of the batched form and its work plan.  See
+// ptf_batch.cu for the design; the kernels are instantiated per (precision,
+// stage) in ptf_batch_inst.cu so they compile in parallel.
+#pragma once
+#include <algorithm>
+#include "ptf_internal.h"
+
+namespace ptf {
+
+constexpr int kBatchThreads = 256;
+constexpr int kMaxBuckets = 32;
+
+template <typename T> struct BucketPlan {
+  ColArgs<T> col;
+  RowArgs<T> row;
+  int n;
+  int row_items, col_items;
+  int row_begin, col_begin;  // first global item of the bucket's row / column tiles
+};
+template <typename T> struct BatchPlan {
+  int nb, row_total, total;
+  BucketPlan<T> b[kMaxBuckets];
+};
+
+#define PTF_BATCH_SIZES(X) X(64) X(128) X(256) X(512) X(1024)
+
+template <typename T> struct BatchBounds { static constexpr int blocks = 1; };
+template <> struct BatchBounds<float> { static constexpr int blocks = 2; };
+
+template <typename T, int N> __host__ __device__ constexpr size_t batch_smem_n() {
+  // W = P = 256 / (N/E) lines per block for both passes
+  return col_smem_bytes<T, N>(kBatchThreads / pass_tpl<T, N>()) > row_smem_bytes<T, N>(kBatchThreads / pass_tpl<T, N>(), 1)
+             ? col_smem_bytes<T, N>(kBatchThreads / pass_tpl<T, N>())
+             : row_smem_bytes<T, N>(kBatchThreads / pass_tpl<T, N>(), 1);
+}
+template <typename T> size_t batch_smem_bytes() {
+  size_t m = 0;
+#define PTF_MAXS(n) m = std::max(m, batch_smem_n<T, n>());
+  PTF_BATCH_SIZES(PTF_MAXS)
+#undef PTF_MAXS
+  return m;
+}
+
+constexpr unsigned long long kSpinLimit = 1ull << 24;  // x 128 ns sleeps: about 2 s
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kBatchThreads, BatchBounds<T>::blocks)
+batch_stage_kernel(const BatchPlan<T>* __restrict__ plan, unsigned int* ctr, int* err, T stage_c) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_item, s_ok;
+  const int nb = plan->nb, row_total = plan->row_total, total = plan->total;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = (int)atomicAdd(&ctr[0], 1u);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= total) return;  // uniform
+    if (item < row_total) {
+      int b = 0;
+      while (b + 1 < nb && item >= plan->b[b + 1].row_begin) ++b;
+      RowArgs<T> ra = plan->b[b].row;
+      ra.stage_c = stage_c;
+      const int local = item - plan->b[b].row_begin;
+      switch (plan->b[b].n) {
+#define PTF_CASE(n) case n: row_body<T, n, true>(ra, local, 0, smem); break;
+        PTF_BATCH_SIZES(PTF_CASE)
+#undef PTF_CASE
+        default: break;
+      }
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) atomicAdd(&ctr[1 + b], 1u);
+    } else {
+      int b = 0;
+      while (b + 1 < nb && item >= plan->b[b + 1].col_begin) ++b;
+      if (threadIdx.x == 0) {
+        const unsigned need = (unsigned)plan->b[b].row_items;
+        unsigned long long spins = 0;
+        int ok = 1;
+        while (*((volatile unsigned int*)&ctr[1 + b]) < need) {
+          if (++spins > kSpinLimit) { atomicExch(err, 1); ok = 0; break; }
+          __nanosleep(128);
+        }
+        __threadfence();
+        s_ok = ok;
+      }
+      __syncthreads();
+      if (s_ok) {
+        ColArgs<T> ca = plan->b[b].col;
+        const int local = item - plan->b[b].col_begin;
+        switch (plan->b[b].n) {
+#define PTF_CASE(n) case n: col_body<T, n, MODE, true>(ca, local, 0, smem); break;
+          PTF_BATCH_SIZES(PTF_CASE)
+#undef PTF_CASE
+          default: break;
+        }
+      }
+    }
+    __syncthreads();  // s_item / s_ok are rewritten by the next item
+  }
+}
+
+// Launcher and set-up of one (precision, stage) kernel; instantiated in
+// ptf_batch_inst.cu objects.
+template <typename T, int MODE>
+cudaError_t launch_batch_stage(const BatchPlan<T>* plan, unsigned int* ctr, int* err, T stage_c, int grid, size_t smem,
+                               cudaStream_t st) {
+  batch_stage_kernel<T, MODE><<<grid, kBatchThreads, smem, st>>>(plan, ctr, err, stage_c);
+  return cudaGetLastError();
+}
+template <typename T, int MODE> cudaError_t setup_batch_stage(size_t smem, int* occ) {
+  cudaError_t e = cudaFuncSetAttribute(batch_stage_kernel<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, batch_stage_kernel<T, MODE>, kBatchThreads, smem);
+}
+template <typename T> __global__ void batch_clock_kernel(SlotParams<T>* slots, int n);
+
+}  // namespace ptf

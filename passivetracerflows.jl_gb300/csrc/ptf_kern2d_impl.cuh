@@ -42,7 +42,7 @@ template <typename T, int N> struct PassLaunch {
   }
   static cudaError_t row(const RowArgs<T>& a, int P, int nby, int batch, cudaStream_t st) {
     if (P * pass_tpl<T, N>() > max_threads(row_pass_kernel<T, N>)) return cudaErrorInvalidConfiguration;
-    const size_t smem = row_smem_bytes<T, N>(P);
+    const size_t smem = row_smem_bytes<T, N>(P, a.park_slots < 1 ? 1 : a.park_slots);
     cudaError_t e = cudaFuncSetAttribute(row_pass_kernel<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     row_pass_kernel<T, N><<<dim3(nby, batch), dim3(P * pass_tpl<T, N>()), smem, st>>>(a);
@@ -52,7 +52,7 @@ template <typename T, int N> struct PassLaunch {
 
 template <typename T, int N> int max_lines_n(bool col) {
   typedef typename cplx_of<T>::type C;
-  const size_t lb = col ? col_smem_bytes<T, N>(1) : row_smem_bytes<T, N>(1);
+  const size_t lb = col ? col_smem_bytes<T, N>(1) : row_smem_bytes<T, N>(1, 2);
   (void)sizeof(C);
   int m = (int)((200u * 1024u) / lb);
   const int tpl = pass_tpl<T, N>();

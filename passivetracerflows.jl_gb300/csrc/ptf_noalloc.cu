@@ -149,7 +149,7 @@ int ptf_calcN2d_noalloc(int32_t nx, int32_t ny, double Lx, double Ly, const doub
   std::memset(&ra, 0, sizeof(ra));
   ra.A = A; ra.B = B; ra.out = NX; ra.u = U; ra.v = V; ra.tw = twx;
   ra.dkx = 2 * M_PI / Lx; ra.scale = 1.0;
-  ra.rows = ny; ra.pitch = pitch; ra.mode = ROW_RHS;
+  ra.rows = ny; ra.pitch = pitch; ra.mode = ROW_RHS; ra.park_slots = 1;
   e = launch_row<double>(nx, ra, P, (ny / 2) / P, 1, st);
   if (e != cudaSuccess) return fail(PTF_ERR_CUDA, std::string("row pass: ") + cudaGetErrorString(e));
   ColArgs<double> cf;

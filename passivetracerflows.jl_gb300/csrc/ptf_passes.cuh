@@ -36,6 +36,24 @@ enum ColMode : int {
 constexpr int COL_NMODES = 12;
 enum RowMode : int { ROW_RHS = 0, ROW_C2R = 1, ROW_R2C = 2, ROW_RHS3 = 3 };
 
+enum FlowKind : int { FLOW_ARRAYS = 0, FLOW_CELLULAR = 1 };
+
+// Per-solve parameters of the batched form (one entry per slot of a bucket
+// of equally sized square 2D solves).  The clock (t, step) advances on the
+// device after every step; a solve that reaches nsteps is deactivated and
+// its state is no longer written.
+template <typename T> struct SlotParams {
+  double t;                 // clock.t at the start of the current step
+  double dtd;               // dt in FP64 (the clock advances by it)
+  long long step, nsteps;   // clock.step and the solve's target
+  T kappa, eta, kappah;     // L = -(kappa kr^2 + eta l^2 + kappah |k|^(2 nkappah))
+  T dt;
+  T dkx, dky;               // 2 pi / Lx, 2 pi / Ly
+  T U, eps, omega;          // FLOW_CELLULAR: psi = U cos(Kx x + eps sin(omega t)) cos(Ky y)
+  int nkappah, active, flow_kind, time_mode;
+  int Kx, Ky;
+};
+
 template <typename T> struct ColArgs {
   typedef typename cplx_of<T>::type C;
   const C* nxin;   // forward input
@@ -57,6 +75,11 @@ template <typename T> struct ColArgs {
   long long bstride;    // elements between blockIdx.y blocks of fields
   long long tplane;     // elements of one table plane
   int tab_per_block;    // 1: tables advance with blockIdx.y (per-solve tables)
+  // batched form only: per-slot parameters, the slots to process
+  // (slot_list[k], k < nslots) and columns per slot
+  const SlotParams<T>* slots;
+  const int* slot_list;
+  int nslots, slot_cols;
 };
 
 template <typename T> struct RowArgs {
@@ -73,7 +96,14 @@ template <typename T> struct RowArgs {
   const C* tw;     // NX-point twiddles
   T dkx, scale;    // scale: C2R normalisation / R2C 1/2 / RHS 1
   int rows, pitch, mode;
+  int park_slots;  // parking slots per point: 1 (2D) or 2 (3D)
   long long bstride, pstride, fstride;
+  // batched form only
+  const SlotParams<T>* slots;
+  const int* slot_list;
+  int nslots;
+  T stage_c;       // stage time offset in units of dt (0, 1/2, 1/2, 1 for RK4)
+  T fscale;        // analytic flow scale: -1/(2 nx ny)
 };
 
 template <typename T, int N>
@@ -102,9 +132,14 @@ template <typename T, int N> __host__ __device__ constexpr size_t col_smem_bytes
 }
 template <typename T, int N> __host__ __device__ constexpr int pass_tpl() { return N / PassE<T, N>::value; }
 
-template <typename T, int N, int MODE>
-__global__ void __launch_bounds__(ColBounds<T>::threads, ColBounds<T>::blocks) col_pass_kernel(ColArgs<T> a) {
+// Body of one column-pass block (tile = column tile index, blk = block of
+// fields).  BATCHED: flat columns run over the slots of a bucket, each
+// thread carries its own slot; the linear operator and dt come from the
+// slot's parameters, and inactive slots are not written.
+template <typename T, int N, int MODE, bool BATCHED>
+__device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk, unsigned char* smem_raw) {
   typedef typename cplx_of<T>::type C;
+  static_assert(!BATCHED || MODE < COL_ETD_1 || MODE >= COL_FWD_N, "the batched form runs RK4");
   constexpr int E = PassE<T, N>::value;
   constexpr int TPL = N / E;
   constexpr int LS = line_stride(N);
@@ -113,15 +148,27 @@ __global__ void __launch_bounds__(ColBounds<T>::threads, ColBounds<T>::blocks) c
   constexpr int RI = FirstRadix<N, +1, E>::value;   // inverse input pattern (== RF)
   constexpr int RO = LastRadix<N, +1, E>::value;    // inverse output pattern
   static_assert(RF == RI, "forward-last and inverse-first radices must match");
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   C* sm = reinterpret_cast<C*>(smem_raw);
   const int W = blockDim.x / TPL;
   const int w = threadIdx.x % W, t = threadIdx.x / W;
-  const int col = blockIdx.x * W + w;
+  int col = tile * W + w;
   const int stride = a.stride;
-  const size_t boff = (size_t)blockIdx.y * (size_t)a.bstride;
+  size_t boff = (size_t)blk * (size_t)a.bstride;
+  bool store = true;
+  T dt = a.dt;
+  int slot = 0;
+  if (BATCHED) {
+    int k = col / a.slot_cols;
+    col -= k * a.slot_cols;
+    store = k < a.nslots;
+    if (!store) k = a.nslots - 1;  // keep loads in bounds; nothing is written
+    slot = a.slot_list[k];
+    store = store && a.slots[slot].active;
+    dt = a.slots[slot].dt;
+    boff = (size_t)slot * (size_t)a.bstride;
+  }
   const size_t plane = (size_t)a.tplane;
-  const size_t toff = a.tab_per_block ? (size_t)blockIdx.y * plane : 0;
+  const size_t toff = a.tab_per_block ? (size_t)blk * plane : 0;
   C* line = sm + w * LS;
   C* park = sm + W * LS;  // slot i of this thread: park[i*blockDim + tid]
   const int nthr = blockDim.x;
@@ -140,7 +187,22 @@ __global__ void __launch_bounds__(ColBounds<T>::threads, ColBounds<T>::blocks) c
   // Stage combination at the positions p = reg_pos<N, RF, E>(t, i); the
   // next stage input is parked (each thread reads back only its own slots,
   // so no barrier is needed).
-  const T dt = a.dt;
+  // Linear operator: table, or (batched) from the slot's parameters.
+  T Lk2 = 0, Lka = 0, Lkb = 0, Lkh = 0;
+  int Lnh = 0;
+  if (BATCHED) {
+    const SlotParams<T>& sp = a.slots[slot];
+    const T kr = (T)col * sp.dkx;
+    Lk2 = kr * kr; Lka = sp.kappa; Lkb = sp.eta; Lkh = sp.kappah; Lnh = sp.nkappah;
+  }
+  auto Lval = [&](const T* Lt, int o, int i) -> T {
+    if (!BATCHED) return Lt[o];
+    const T l = kval<T, N>(reg_pos<N, RF, E>(t, i), a.slots[slot].dky);
+    const T l2 = l * l;
+    T hyp = 0;
+    if (Lkh != 0) { const T K2 = Lk2 + l2; hyp = Lkh; for (int q = 0; q < Lnh; ++q) hyp *= K2; }
+    return -(Lka * Lk2 + Lkb * l2 + hyp);
+  };
   {
     C* __restrict__ S = a.s + boff;
     C* __restrict__ SI = a.si + boff;
@@ -151,64 +213,62 @@ __global__ void __launch_bounds__(ColBounds<T>::threads, ColBounds<T>::blocks) c
 #pragma unroll
     for (int i = 0; i < E; ++i) {
       const int o = PTF_OFF(RF, i);
-      const C N = v[i];
+      const C Nh = v[i];  // forward transform of the RHS at this element
       C x;
       if (MODE == COL_PROLOGUE || MODE == COL_YINV3) {
         x = S[o];
       } else if (MODE == COL_FWD_STORE) {
-        x = N; S[o] = x;
+        x = Nh; if (store) S[o] = x;
       } else if (MODE == COL_FWD_N) {
-        x = N; a.nout[boff + o] = N;
+        x = Nh; if (store) a.nout[boff + o] = Nh;
       } else if (MODE == COL_RK4_1) {
-        const T L = Lt[o];
+        const T L = Lval(Lt, o, i);
         const C s = S[o];
-        C k; k.x = L * s.x + N.x; k.y = L * s.y + N.y;
+        C k; k.x = L * s.x + Nh.x; k.y = L * s.y + Nh.y;
         C ac; ac.x = s.x + (dt / 6) * k.x; ac.y = s.y + (dt / 6) * k.y;
-        AC[o] = ac;
         x.x = s.x + (dt / 2) * k.x; x.y = s.y + (dt / 2) * k.y;
-        SI[o] = x;
+        if (store) { AC[o] = ac; SI[o] = x; }
       } else if (MODE == COL_RK4_2 || MODE == COL_RK4_3) {
-        const T L = Lt[o];
+        const T L = Lval(Lt, o, i);
         const C si = SI[o], s = S[o];
         C ac = AC[o];
-        C k; k.x = L * si.x + N.x; k.y = L * si.y + N.y;
+        C k; k.x = L * si.x + Nh.x; k.y = L * si.y + Nh.y;
         ac.x += (dt / 3) * k.x; ac.y += (dt / 3) * k.y;
-        AC[o] = ac;
         const T h = (MODE == COL_RK4_2) ? dt / 2 : dt;
         x.x = s.x + h * k.x; x.y = s.y + h * k.y;
-        SI[o] = x;
+        if (store) { AC[o] = ac; SI[o] = x; }
       } else if (MODE == COL_RK4_4) {
-        const T L = Lt[o];
+        const T L = Lval(Lt, o, i);
         const C si = SI[o], ac = AC[o];
-        C k; k.x = L * si.x + N.x; k.y = L * si.y + N.y;
+        C k; k.x = L * si.x + Nh.x; k.y = L * si.y + Nh.y;
         x.x = ac.x + (dt / 6) * k.x; x.y = ac.y + (dt / 6) * k.y;
-        S[o] = x;
+        if (store) S[o] = x;
       } else if (MODE == COL_ETD_1) {
         const T Ee = cf[o], E2 = cf[o + plane], ze = cf[o + 2 * plane], al = cf[o + 3 * plane];
         const C s = S[o];
-        N1p[o] = N;
-        C ac; ac.x = Ee * s.x + al * N.x; ac.y = Ee * s.y + al * N.y;
+        N1p[o] = Nh;
+        C ac; ac.x = Ee * s.x + al * Nh.x; ac.y = Ee * s.y + al * Nh.y;
         AC[o] = ac;
-        x.x = E2 * s.x + ze * N.x; x.y = E2 * s.y + ze * N.y;
+        x.x = E2 * s.x + ze * Nh.x; x.y = E2 * s.y + ze * Nh.y;
         SI[o] = x;
       } else if (MODE == COL_ETD_2) {
         const T E2 = cf[o + plane], ze = cf[o + 2 * plane], be = cf[o + 4 * plane];
         const C s = S[o];
         C ac = AC[o];
-        ac.x += 2 * be * N.x; ac.y += 2 * be * N.y;
+        ac.x += 2 * be * Nh.x; ac.y += 2 * be * Nh.y;
         AC[o] = ac;
-        x.x = E2 * s.x + ze * N.x; x.y = E2 * s.y + ze * N.y;
+        x.x = E2 * s.x + ze * Nh.x; x.y = E2 * s.y + ze * Nh.y;
       } else if (MODE == COL_ETD_3) {
         const T E2 = cf[o + plane], ze = cf[o + 2 * plane], be = cf[o + 4 * plane];
         const C s1 = SI[o], N1 = N1p[o];
         C ac = AC[o];
-        ac.x += 2 * be * N.x; ac.y += 2 * be * N.y;
+        ac.x += 2 * be * Nh.x; ac.y += 2 * be * Nh.y;
         AC[o] = ac;
-        x.x = E2 * s1.x + ze * (2 * N.x - N1.x); x.y = E2 * s1.y + ze * (2 * N.y - N1.y);
+        x.x = E2 * s1.x + ze * (2 * Nh.x - N1.x); x.y = E2 * s1.y + ze * (2 * Nh.y - N1.y);
       } else {  // COL_ETD_4
         const T ga = cf[o + 5 * plane];
         const C ac = AC[o];
-        x.x = ac.x + ga * N.x; x.y = ac.y + ga * N.y;
+        x.x = ac.x + ga * Nh.x; x.y = ac.y + ga * Nh.y;
         S[o] = x;
       }
       park[i * nthr + threadIdx.x] = x;
@@ -220,7 +280,7 @@ __global__ void __launch_bounds__(ColBounds<T>::threads, ColBounds<T>::blocks) c
 #pragma unroll
   for (int i = 0; i < E; ++i) v[i] = park[i * nthr + threadIdx.x];
   fft_line<N, +1, E>(v, t, line, a.tw);
-  {
+  if (store) {
     C* __restrict__ Ap = a.A + boff;
 #pragma unroll
     for (int i = 0; i < E; ++i) Ap[PTF_OFF(RO, i)] = v[i];
@@ -231,13 +291,13 @@ __global__ void __launch_bounds__(ColBounds<T>::threads, ColBounds<T>::blocks) c
   // B = F^-1(i k s_next)
 #pragma unroll
   for (int i = 0; i < E; ++i) {
-    const T k = kval<T, N>(reg_pos<N, RI, E>(t, i), a.dk);
+    const T k = kval<T, N>(reg_pos<N, RI, E>(t, i), BATCHED ? a.slots[slot].dky : a.dk);
     const C x = park[i * nthr + threadIdx.x];
     v[i].x = -k * x.y;
     v[i].y = k * x.x;
   }
   fft_line<N, +1, E>(v, t, line, a.tw);
-  {
+  if (store) {
     C* __restrict__ Bp = a.B + boff;
 #pragma unroll
     for (int i = 0; i < E; ++i) Bp[PTF_OFF(RO, i)] = v[i];
@@ -254,6 +314,12 @@ __global__ void __launch_bounds__(ColBounds<T>::threads, ColBounds<T>::blocks) c
     for (int i = 0; i < E; ++i) Cp[PTF_OFF(RO, i)] = v[i];
   }
 #undef PTF_OFF
+}
+
+template <typename T, int N, int MODE>
+__global__ void __launch_bounds__(ColBounds<T>::threads, ColBounds<T>::blocks) col_pass_kernel(ColArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  col_body<T, N, MODE, false>(a, blockIdx.x, blockIdx.y, smem_raw);
 }
 
 // ---------------------------------------------------------------------------
@@ -307,14 +373,61 @@ __device__ __forceinline__ C zsrc_c2r(const C* A0, const C* A1, int k, int NX) {
   return z;
 }
 
-// Shared memory of a row-pass block with P pairs: one FFT line and two
-// parking slots per point of each pair.
-template <typename T, int NX> __host__ __device__ constexpr size_t row_smem_bytes(int P) {
-  return (size_t)P * (line_stride(NX) + 2 * NX) * sizeof(typename cplx_of<T>::type);
+// Shared memory of a row-pass block with P pairs: one FFT line and
+// `slots` parking slots per point of each pair (1 in 2D, 2 in 3D).
+template <typename T, int NX> __host__ __device__ constexpr size_t row_smem_bytes(int P, int slots) {
+  return (size_t)P * (line_stride(NX) + slots * NX) * sizeof(typename cplx_of<T>::type);
 }
 
-template <typename T, int NX>
-__global__ void __launch_bounds__(256) row_pass_kernel(RowArgs<T> a) {
+// exp(i K x_j) on the grid x_j = -L/2 + j L/n for an integer K:
+// (-1)^K conj(tw[(K j) mod n]) with tw[m] = exp(-2 pi i m / n).
+template <typename C>
+__device__ __forceinline__ C grid_expi(const C* __restrict__ tw, int K, int j, int n) {
+  int m = (int)(((long long)K * j) % n);
+  if (m < 0) m += n;
+  const C w = __ldg(tw + m);
+  C r;
+  r.x = w.x; r.y = -w.y;
+  if (K & 1) { r.x = -r.x; r.y = -r.y; }
+  return r;
+}
+__device__ __forceinline__ void sin_cos(double x, double* s, double* c) { sincos(x, s, c); }
+__device__ __forceinline__ void sin_cos(float x, float* s, float* c) { sincosf(x, s, c); }
+
+// The scaled cellular flow psi = U cos(Kx x + eps sin(omega t)) cos(Ky y) of a
+// slot at one row: u = -d(psi)/dy, v = d(psi)/dx, times fscale.
+template <typename T> struct CellularRow {
+  T cphi, sphi, au, av, sy, cy;
+  int Kx;
+};
+template <typename T, typename C>
+__device__ __forceinline__ CellularRow<T> cellular_row(const SlotParams<T>& sp, const C* tw, int yrow, int n,
+                                                        T stage_c, T fscale) {
+  CellularRow<T> r;
+  const double te = sp.t + (sp.time_mode ? (double)stage_c * (double)sp.dt : 0.0);
+  const T phi = sp.eps * (T)sin((double)sp.omega * te);
+  sin_cos(phi, &r.sphi, &r.cphi);
+  const C ey = grid_expi(tw, sp.Ky, yrow, n);
+  r.cy = ey.x; r.sy = ey.y;
+  const T kx = (T)sp.Kx * sp.dkx, ky = (T)sp.Ky * sp.dky;
+  r.au = fscale * sp.U * ky;    // u =  U ky cos(kx x + phi) sin(ky y)
+  r.av = -fscale * sp.U * kx;   // v = -U kx sin(kx x + phi) cos(ky y)
+  r.Kx = sp.Kx;
+  return r;
+}
+template <typename T, typename C>
+__device__ __forceinline__ void cellular_uv(const CellularRow<T>& r, const C* tw, int x, int n, T* u, T* v) {
+  const C e = grid_expi(tw, r.Kx, x, n);
+  const T ct = e.x * r.cphi - e.y * r.sphi, st = e.y * r.cphi + e.x * r.sphi;
+  *u = r.au * ct * r.sy;
+  *v = r.av * st * r.cy;
+}
+
+// Body of one row-pass block (tile = pair tile index, blk = block of fields).
+// BATCHED: flat pairs run over the slots of a bucket; each thread carries
+// its slot, whose flow is an array or the analytic cellular flow.
+template <typename T, int NX, bool BATCHED>
+__device__ __forceinline__ void row_body(const RowArgs<T>& a, int tile, int blk, unsigned char* smem_raw) {
   typedef typename cplx_of<T>::type C;
   constexpr int E = PassE<T, NX>::value;
   constexpr int TPL = NX / E;
@@ -324,19 +437,32 @@ __global__ void __launch_bounds__(256) row_pass_kernel(RowArgs<T> a) {
   constexpr int RF0 = FirstRadix<NX, -1, E>::value;  // == E
   constexpr int RFL = LastRadix<NX, -1, E>::value;
   static_assert(RIL == RF0, "inverse-last and forward-first radices must match");
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   C* sm = reinterpret_cast<C*>(smem_raw);
   const int P = blockDim.x / TPL;
   const int pr = threadIdx.x / TPL, t = threadIdx.x % TPL;
-  const int y0 = 2 * (blockIdx.x * P + pr);
-  const long long boff = (long long)blockIdx.y * a.bstride;
-  const long long poff = (long long)blockIdx.y * a.pstride;
-  const long long foff = (long long)blockIdx.y * a.fstride;
+  int y0 = 2 * (tile * P + pr);
+  long long boff = (long long)blk * a.bstride;
+  long long poff = (long long)blk * a.pstride;
+  long long foff = (long long)blk * a.fstride;
+  bool valid = y0 < a.rows;  // grids are sized exactly; kept for safety
+  int slot = 0;
+  if (BATCHED) {
+    const int pair = y0 / 2, pps = a.rows / 2;
+    int k = pair / pps;
+    y0 = 2 * (pair - k * pps);
+    valid = k < a.nslots;
+    if (!valid) k = a.nslots - 1;  // keep loads in bounds; nothing is written
+    slot = a.slot_list[k];
+    valid = valid && a.slots[slot].active;
+    boff = (long long)slot * a.bstride;
+    poff = (long long)slot * a.pstride;
+    foff = (long long)slot * a.fstride;
+  }
   const int pitch = a.pitch;
   C* line = sm + pr * LS;
-  C* park = sm + P * LS + pr * 2 * NX;  // this pair's slots: park[i*TPL + t], park[NX + i*TPL + t]
-  const bool valid = y0 < a.rows;  // grids are sized exactly; kept for safety
-  const int yy0 = valid ? y0 : 0;
+  // this pair's parking slots: park[i*TPL + t] (and park[NX + i*TPL + t] in 3D)
+  C* park = sm + P * LS + pr * a.park_slots * NX;
+  const int yy0 = (BATCHED || valid) ? y0 : 0;
   const long long r0 = boff + (long long)yy0 * pitch, r1 = r0 + pitch;
   const long long q0 = (long long)yy0 * NX, q1 = q0 + NX;
 
@@ -372,32 +498,57 @@ __global__ void __launch_bounds__(256) row_pass_kernel(RowArgs<T> a) {
       for (int i = 0; i < E; ++i) park[NX + i * TPL + t] = v[i];
       asm volatile("" ::: "memory");
     }
+    const bool analytic = BATCHED && a.slots[slot].flow_kind == FLOW_CELLULAR;
     // row y0: c_x + i c_y -> park the product's first half
 #pragma unroll
     for (int i = 0; i < E; ++i) v[i] = zsrc_rhs<T, C>(a.A + r0, a.B + r0, reg_pos<NX, RI0, E>(t, i), NX, a.dkx);
     fft_line<NX, +1, E>(v, t, line, a.tw);
+    if (analytic) {
+      const CellularRow<T> cr = cellular_row<T, C>(a.slots[slot], a.tw, yy0, NX, a.stage_c, a.fscale);
 #pragma unroll
-    for (int i = 0; i < E; ++i) {
-      const int x = reg_pos<NX, RIL, E>(t, i);
-      T n0 = a.u[foff + q0 + x] * v[i].x + a.v[foff + q0 + x] * v[i].y;
-      if (three) n0 += a.w[foff + q0 + x] * park[NX + i * TPL + t].x;
-      C pk; pk.x = n0; pk.y = 0;
-      park[i * TPL + t] = pk;
+      for (int i = 0; i < E; ++i) {
+        T uu, vv;
+        cellular_uv<T, C>(cr, a.tw, reg_pos<NX, RIL, E>(t, i), NX, &uu, &vv);
+        C pk; pk.x = uu * v[i].x + vv * v[i].y; pk.y = 0;
+        park[i * TPL + t] = pk;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        const int x = reg_pos<NX, RIL, E>(t, i);
+        T n0 = a.u[foff + q0 + x] * v[i].x + a.v[foff + q0 + x] * v[i].y;
+        if (three) n0 += a.w[foff + q0 + x] * park[NX + i * TPL + t].x;
+        C pk; pk.x = n0; pk.y = 0;
+        park[i * TPL + t] = pk;
+      }
     }
     asm volatile("" ::: "memory");
     // row y1
 #pragma unroll
     for (int i = 0; i < E; ++i) v[i] = zsrc_rhs<T, C>(a.A + r1, a.B + r1, reg_pos<NX, RI0, E>(t, i), NX, a.dkx);
     fft_line<NX, +1, E>(v, t, line, a.tw);
+    if (analytic) {
+      const CellularRow<T> cr = cellular_row<T, C>(a.slots[slot], a.tw, yy0 + 1, NX, a.stage_c, a.fscale);
 #pragma unroll
-    for (int i = 0; i < E; ++i) {
-      const int x = reg_pos<NX, RIL, E>(t, i);
-      T n1 = a.u[foff + q1 + x] * v[i].x + a.v[foff + q1 + x] * v[i].y;
-      if (three) n1 += a.w[foff + q1 + x] * park[NX + i * TPL + t].y;
-      C w;
-      w.x = park[i * TPL + t].x;
-      w.y = n1;
-      v[i] = w;
+      for (int i = 0; i < E; ++i) {
+        T uu, vv;
+        cellular_uv<T, C>(cr, a.tw, reg_pos<NX, RIL, E>(t, i), NX, &uu, &vv);
+        C w;
+        w.x = park[i * TPL + t].x;
+        w.y = uu * v[i].x + vv * v[i].y;
+        v[i] = w;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        const int x = reg_pos<NX, RIL, E>(t, i);
+        T n1 = a.u[foff + q1 + x] * v[i].x + a.v[foff + q1 + x] * v[i].y;
+        if (three) n1 += a.w[foff + q1 + x] * park[NX + i * TPL + t].y;
+        C w;
+        w.x = park[i * TPL + t].x;
+        w.y = n1;
+        v[i] = w;
+      }
     }
   }
   // forward x-FFT of n_y0 + i n_y1
@@ -419,6 +570,12 @@ __global__ void __launch_bounds__(256) row_pass_kernel(RowArgs<T> a) {
       a.out[r1 + k] = o1;
     }
   }
+}
+
+template <typename T, int NX>
+__global__ void __launch_bounds__(256) row_pass_kernel(RowArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  row_body<T, NX, false>(a, blockIdx.x, blockIdx.y, smem_raw);
 }
 
 }  // namespace ptf
