@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--serve-requests-fp64", type=int, default=48)
     ap.add_argument("--serve-rate", type=float, default=40.0, help="Poisson arrival rate (requests/s)")
     ap.add_argument("--ensemble-steps", type=int, default=100)
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes (no ptf_autotune)")
+    ap.add_argument("--no-comparator", action="store_true", help="skip the torch/cuFFT comparator")
     return ap.parse_args()
 
 
@@ -175,6 +177,78 @@ def cpu_oracle_rate(args, seconds, max_steps):
     return args.n * args.n * steps / el, steps, el, o.WORKERS
 
 
+# ---------------------------------------------------------------------------
+# GPU comparator: the reference's GPU operation sequence restated with
+# torch.fft (cuFFT) and eager elementwise kernels -- what FourierFlows does on
+# CUDA.jl for this module: calcN! = two c2r transforms of (i kr s, i l s), the
+# product with the flow, one r2c (src/traceradvectiondiffusion.jl:756-769),
+# with ETDRK4's stage arithmetic as separate broadcasts.  Not the product;
+# reported beside it.
+# ---------------------------------------------------------------------------
+def etdrk4_tables(torch, Lh, dt, npts=32):
+    """Kassam & Trefethen (2005) contour-integral ETDRK4 coefficients (FP64)."""
+    r = torch.exp(1j * np.pi * (torch.arange(1, npts + 1, dtype=torch.float64, device=Lh.device) - 0.5) / npts)
+    out = {"E": torch.exp(dt * Lh), "E2": torch.exp(dt * Lh / 2)}
+    q, f1, f2, f3 = (torch.zeros_like(Lh) for _ in range(4))
+    for k in range(npts):
+        z = dt * Lh.to(torch.complex128) + r[k]
+        ez = torch.exp(z)
+        q += ((torch.exp(z / 2) - 1) / z).real
+        f1 += ((-4 - z + ez * (4 - 3 * z + z * z)) / z ** 3).real
+        f2 += ((2 + z + ez * (z - 2)) / z ** 3).real
+        f3 += ((-4 - 3 * z - z * z + ez * (4 - z)) / z ** 3).real
+    out.update(Q=dt * q / npts, f1=dt * f1 / npts, f2=dt * f2 / npts, f3=dt * f3 / npts)
+    return out
+
+
+def torch_comparator(torch, n, batch, dt, steps, c0, flush=None, dtype=None):
+    dev = "cuda"
+    rdt = dtype or torch.float64
+    L = 2 * np.pi
+    x = torch.tensor(-L / 2 + L / n * np.arange(n), dtype=torch.float64, device=dev)
+    Y, X = torch.meshgrid(x, x, indexing="ij")
+    u = (4.0 * torch.cos(4 * X) * torch.sin(4 * Y)).to(rdt)
+    v = (-4.0 * torch.sin(4 * X) * torch.cos(4 * Y)).to(rdt)
+    kr = torch.arange(n // 2 + 1, dtype=torch.float64, device=dev) * (2 * np.pi / L)
+    ll = torch.fft.fftfreq(n, d=1.0 / n, dtype=torch.float64, device=dev) * (2 * np.pi / L)
+    K2 = kr[None, :] ** 2 + ll[:, None] ** 2
+    Lh = -1e-4 * kr[None, :] ** 2 - 1e-4 * ll[:, None] ** 2 - 1e-12 * K2 ** 2
+    tb = {k: t.to(rdt) for k, t in etdrk4_tables(torch, Lh, dt).items()}
+    ikr = (1j * kr[None, :]).to(torch.complex64 if rdt == torch.float32 else torch.complex128)
+    il = (1j * ll[:, None]).to(ikr.dtype)
+
+    def calcN(sh):
+        cx = torch.fft.irfft2(ikr * sh, s=(n, n))
+        cy = torch.fft.irfft2(il * sh, s=(n, n))
+        return torch.fft.rfft2(-(u * cx + v * cy))
+
+    def step(s):
+        N1 = calcN(s)
+        a = tb["E2"] * s + tb["Q"] * N1
+        Na = calcN(a)
+        b = tb["E2"] * s + tb["Q"] * Na
+        Nb = calcN(b)
+        c = tb["E2"] * a + tb["Q"] * (2 * Nb - N1)
+        Nc = calcN(c)
+        return tb["E"] * s + tb["f1"] * N1 + 2 * tb["f2"] * (Na + Nb) + tb["f3"] * Nc
+
+    s = torch.fft.rfft2(torch.as_tensor(c0, device=dev).reshape(batch, n, n).to(rdt))
+    for _ in range(3):
+        s = step(s)
+    torch.cuda.synchronize()
+    ms = 0.0
+    for _ in range(steps):
+        if flush is not None:
+            flush.fill_(1.0)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        s = step(s)
+        b.record()
+        b.synchronize()
+        ms += a.elapsed_time(b)
+    return batch * n * n * steps / (ms / 1e3), ms / steps, step, s
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -246,6 +320,7 @@ def run_ours(args):
     p32 = pkg.Problem(pkg.GPU(), pkg.TwoDAdvectingFlow(u=u, v=v), T=np.float32, batch=B, **kw)
     pkg.set_c(p32, c0)
     st32 = torch.cuda.ExternalStream(p32.stream)
+    tuning32 = p32.autotune(trial_steps=4) if not args.no_tune else p32.tuning
     pkg.stepforward(p32, W)
     sampler = ClockSampler(torch.cuda.current_device())
     sampler.start()
@@ -261,7 +336,9 @@ def run_ours(args):
     ms32 = max_over_ranks(e0.elapsed_time(e1))
     launches = p32.kernel_launches - launches0
     value = world * B * n * n * K / (ms32 / 1e3)
-    # per-pass roofline (same stream, CUDA events around each pass)
+    # per-pass roofline (CUDA events around each pass; one branch, so that
+    # the events of concurrent passes do not overlap)
+    p32.tuning = dict(branches=1, solves_per_group=0)
     lib.ptf_profile(p32._h, 1)
     pkg.stepforward(p32, K)
     prof = {}
@@ -269,11 +346,13 @@ def run_ours(args):
         ms, cnt, by = ct_read(lib, p32._h, kind)
         prof[name] = {"ms": ms, "launches": cnt, "bytes": by}
     lib.ptf_profile(p32._h, 0)
+    p32.tuning = {k: v for k, v in tuning32.items() if k != "ms_per_step"}
     steps32 = W + 2 * K
     # ---------------- FP64 plain ----------------
     p64 = pkg.Problem(pkg.GPU(), pkg.TwoDAdvectingFlow(u=u, v=v), T=np.float64, batch=1, **kw)
     pkg.set_c(p64, c0[0])
     st64 = torch.cuda.ExternalStream(p64.stream)
+    tuning64 = p64.autotune(trial_steps=4) if not args.no_tune else p64.tuning
     pkg.stepforward(p64, W)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     K64 = K
@@ -326,6 +405,34 @@ def run_ours(args):
             "mass_drift_oracle": float(po.vars.c.sum()) / m0 - 1,
             "oracle_seconds": time.perf_counter() - t0,
         }
+    # ---------------- torch/cuFFT restatement of the reference's GPU sequence ----------------
+    comparator = None
+    if rank == 0 and not args.no_comparator:
+        try:
+            KC = max(3, min(K, 20))
+            v32, ms32c, _, _ = torch_comparator(torch, n, B, dt, KC, c0, dtype=torch.float32)
+            v64c, ms64c, step64, _ = torch_comparator(torch, n, 1, dt, KC, c0[0], flush=flush)
+            # same algorithm: a fresh FP64 comparator solve against a fresh FP64 solve of ours, 3 steps
+            s = torch.fft.rfft2(torch.as_tensor(c0[0], device="cuda").reshape(1, n, n))
+            for _ in range(3):
+                s = step64(s)
+            cref = torch.fft.irfft2(s, s=(n, n))[0].cpu().numpy()
+            q = pkg.Problem(pkg.GPU(), pkg.TwoDAdvectingFlow(u=u, v=v), T=np.float64, batch=1, **kw)
+            pkg.set_c(q, c0[0])
+            pkg.stepforward(q, 3)
+            pkg.updatevars(q)
+            agree = float(np.linalg.norm(q.vars.c - cref) / np.linalg.norm(cref))
+            del q
+            comparator = {
+                "what": "reference GPU op sequence restated in torch.fft (cuFFT) + eager elementwise kernels",
+                "fp32_batched": {"value": v32, "unit": UNIT, "ms_per_step": ms32c, "batch": B},
+                "fp64_plain": {"value": v64c, "unit": UNIT, "ms_per_step": ms64c, "batch": 1},
+                "steps": KC, "rel_l2_fp64_vs_ours_3_steps": agree,
+                "ours_over_comparator_fp32": value / v32, "ours_over_comparator_fp64": value64 / v64c,
+            }
+        except Exception as e:
+            comparator = {"error": f"{type(e).__name__}: {e}"}
+        torch.cuda.empty_cache()
     # ---------------- end to end through the public API ----------------
     S = min(25, K)
     frames = max(1, K // S)
@@ -384,9 +491,11 @@ def run_ours(args):
         "ms_per_step": ms32 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded Gaussian ensemble on the cellular flow)",
         "config": dict(workload(args, B), parallelism="replicas" if world > 1 else "single GPU"),
+        "tuning": {"fp32_batched": tuning32, "fp64_plain": tuning64},
         "fp64_plain": {"value": value64, "unit": UNIT, "ms_per_step": ms64 / K64, "steps": K64, "dtype": "f64",
                        "passes": passes64, "ratio_fp32_batched_over_fp64": value / value64},
         "accuracy": acc,
+        "gpu_comparator": comparator,
         "passes": passes,
         "roofline": roof,
         "cpu_baseline": cpu,

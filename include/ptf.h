@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define PTF_ABI_VERSION 1
+#define PTF_ABI_VERSION 2
 
 enum ptf_status {
   PTF_OK = 0,
@@ -67,12 +67,15 @@ typedef struct ptf_config {
   int32_t precision; /* ptf_precision */
   int32_t time_mode; /* ptf_time_mode */
   int32_t batch;     /* independent solves sharing grid, parameters and flow */
+  int32_t k0_mode;   /* FP32 only: 1 (default) carries the conserved (0,0[,0])
+                        mode -- its state and stage combinations -- in FP64,
+                        with N(0,0) a compensated FP64 sum; 0: all FP32 */
 } ptf_config;
 
 typedef struct ptf_handle ptf_handle;
 
 /* Fill a config with the reference's defaults: nx=ny=nz=128, L=2pi,
- * kappa=0.1, eta=iota=kappa, dt=0.01, RK4, FP64, batch 1. */
+ * kappa=0.1, eta=iota=kappa, dt=0.01, RK4, FP64, batch 1, k0_mode 1. */
 void ptf_config_default(ptf_config* cfg, int32_t dim);
 
 /* TracerAdvectionDiffusion.Problem(dev, flow; ...) construction:
@@ -114,6 +117,36 @@ int ptf_get_stream(const ptf_handle* h, void** stream);
 int ptf_set_stream(ptf_handle* h, void* stream);
 /* Bytes of device memory held by the handle. */
 int ptf_device_bytes(const ptf_handle* h, int64_t* bytes);
+/* Step schedule (no reference counterpart).  A batched handle runs each step
+ * in groups of solves_per_group solves (0: the whole batch, or batch/branches
+ * with several branches); groups are dealt to `branches` (1..4) concurrent
+ * stream branches that fork from and join back to the handle's stream.  With
+ * use_graph != 0, ptf_step(h, n > 1) captures one step as a CUDA graph and
+ * replays it.  The schedule does not change results. */
+int ptf_set_schedule(ptf_handle* h, int32_t solves_per_group, int32_t branches, int32_t use_graph);
+/* Launch shapes of a handle (no reference counterpart).  col_lines: columns
+ * per column-pass block of the main column pass (y in 2D, z in 3D);
+ * col_lines_y: the same for the 3D y passes (0 in 2D); row_pairs: row pairs
+ * per row-pass block; branches / solves_per_group: as ptf_set_schedule;
+ * row_staged: 2D RHS row pass staging its rows in shared memory with bulk
+ * copies (falls back to the direct kernel where that does not fit);
+ * ms_per_step: the time measured by ptf_autotune (0 when not tuned).  Line
+ * counts are powers of two dividing the lines of the pass, within the
+ * block's resource limit.  Shapes do not change results. */
+typedef struct ptf_tuning {
+  int32_t col_lines, col_lines_y, row_pairs, branches, solves_per_group, row_staged;
+  double ms_per_step;
+} ptf_tuning;
+enum { PTF_TUNE_FORCE = 1 };
+int ptf_get_tuning(const ptf_handle* h, ptf_tuning* out);
+int ptf_set_tuning(ptf_handle* h, const ptf_tuning* t);
+/* Pick the launch shapes by timing trial_steps steps per candidate on this
+ * handle, one shape at a time (columns per block, 3D y columns, row pairs,
+ * branches, staged row pass), keeping the fastest.  The solution, clock and
+ * step count are saved and restored, so the solve is unchanged.  Choices are
+ * cached per (precision, grid, batch, stepper, k0_mode) for the process and
+ * reused unless flags has PTF_TUNE_FORCE.  Needs the flow to be set. */
+int ptf_autotune(ptf_handle* h, int32_t trial_steps, int32_t flags);
 /* Per-pass timing: with enable != 0 every pass launch is bracketed by CUDA
  * events on the handle's stream (enabling or disabling clears the record).
  * ptf_profile_read sums, for kind 0 (column passes: y transforms + stepper

@@ -26,7 +26,7 @@ class PtfConfig(ct.Structure):
         ("kappah", ct.c_double), ("nkappah", ct.c_int32),
         ("dt", ct.c_double),
         ("stepper", ct.c_int32), ("precision", ct.c_int32), ("time_mode", ct.c_int32),
-        ("batch", ct.c_int32),
+        ("batch", ct.c_int32), ("k0_mode", ct.c_int32),
     ]
 
 
@@ -59,6 +59,15 @@ class PtfServerStats(ct.Structure):
     _fields_ = [("completed", ct.c_int64), ("failed", ct.c_int64), ("queued", ct.c_int64), ("active", ct.c_int64),
                 ("p50_s", ct.c_double), ("p99_s", ct.c_double), ("mean_s", ct.c_double),
                 ("grid_point_steps", ct.c_double), ("wall_s", ct.c_double), ("device_bytes", ct.c_int64)]
+
+
+class PtfTuning(ct.Structure):
+    _fields_ = [("col_lines", ct.c_int32), ("col_lines_y", ct.c_int32), ("row_pairs", ct.c_int32),
+                ("branches", ct.c_int32), ("solves_per_group", ct.c_int32), ("row_staged", ct.c_int32),
+                ("ms_per_step", ct.c_double)]
+
+
+PTF_TUNE_FORCE = 1
 
 
 class PtfError(RuntimeError):
@@ -123,6 +132,10 @@ SIGNATURES = {
     "ptf_server_release": (ct.c_int, [ct.c_void_p, ct.c_int64]),
     "ptf_server_wait_all": (ct.c_int, [ct.c_void_p, ct.c_double]),
     "ptf_server_get_stats": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfServerStats)]),
+    "ptf_set_schedule": (ct.c_int, [ct.c_void_p, ct.c_int32, ct.c_int32, ct.c_int32]),
+    "ptf_get_tuning": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfTuning)]),
+    "ptf_set_tuning": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfTuning)]),
+    "ptf_autotune": (ct.c_int, [ct.c_void_p, ct.c_int32, ct.c_int32]),
     "ptf_profile": (ct.c_int, [ct.c_void_p, ct.c_int32]),
     "ptf_profile_read": (ct.c_int, [ct.c_void_p, ct.c_int32, ct.POINTER(ct.c_double), ct.POINTER(ct.c_int64),
                                     ct.POINTER(ct.c_double)]),

@@ -16,9 +16,12 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -127,6 +130,25 @@ struct ptf_handle {
   bool ab_valid = false, have_c = false, have_flow = false;
   ColGeom gmain, gy3;  // main column pass (y in 2D, z in 3D); 3D y passes
   int rowP = 1;
+  // schedule: solves per group (a step runs all its passes group by group so
+  // a group's fields stay in L2), and a CUDA graph of one step
+  int* err_dev = nullptr;  // device error flag of bounded waits
+  // FP64 k = 0 mode (FP32 handles): per solve {s, stage input, acc, N1} of
+  // the (0,0[,0]) mode, then 64 sum partials per solve and one sum per
+  // solve; k0c = FP64 {L, E, E2, zeta, alpha, beta, gamma} at (0,0[,0])
+  bool k0mode = false;
+  double* k0 = nullptr;
+  double* k0c = nullptr;
+  int row_tma = 0;         // 2D RHS row pass with bulk-copy staging (tuning variant)
+  int group = 0;           // 0: automatic
+  int branches = 1;        // groups run as this many concurrent stream branches
+  int use_graph = 1;
+  double tuned_ms = 0.0;   // ms per step of the tuned shapes (0: not tuned)
+  cudaStream_t side[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join[3] = {nullptr, nullptr, nullptr};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int graph_group = -1;
   long long bytes = 0;
   long long launches = 0;
   std::string err;
@@ -202,6 +224,15 @@ template <typename T> int upload_tables(ptf_handle* h) {
   for (size_t i = 0; i < plane; ++i) Lt[i] = (T)L[i];
   int rc = upload(h, h->Ltab, Lt, "upload L");
   if (rc) return rc;
+  if (h->k0mode) {
+    // the (0,0[,0]) mode's operator and ETDRK4 coefficients in FP64
+    const double L0 = L[0], dt = c.dt;
+    double ph[4];
+    etd_phis(dt * L0, ph);
+    const std::vector<double> kc = {L0, std::exp(dt * L0), std::exp(dt * L0 / 2), dt * ph[0], dt * ph[1],
+                                    dt * ph[2], dt * ph[3], 0.0};
+    if ((rc = upload(h, h->k0c, kc, "upload k = 0 coefficients"))) return rc;
+  }
   if (c.stepper == PTF_ETDRK4) {
     std::vector<T> cf(6 * plane, (T)0);
     const double dt = c.dt;
@@ -276,16 +307,16 @@ cudaEvent_t pool_event(ptf_handle* h) {
   cudaEventCreate(&e);
   return e;
 }
-void prof_begin(ptf_handle* h, cudaEvent_t* e0) {
+void prof_begin(ptf_handle* h, cudaEvent_t* e0, cudaStream_t st) {
   *e0 = nullptr;
   if (!h->profiling) return;
   *e0 = pool_event(h);
-  cudaEventRecord(*e0, h->stream);
+  cudaEventRecord(*e0, st);
 }
-void prof_end(ptf_handle* h, cudaEvent_t e0, int kind, double bytes) {
+void prof_end(ptf_handle* h, cudaEvent_t e0, int kind, double bytes, cudaStream_t st) {
   if (!h->profiling || !e0) return;
   cudaEvent_t e1 = pool_event(h);
-  cudaEventRecord(e1, h->stream);
+  cudaEventRecord(e1, st);
   h->prof.push_back({kind, e0, e1, bytes});
 }
 void prof_clear(ptf_handle* h) {
@@ -306,24 +337,42 @@ struct ColIO {
   void* nout = nullptr;
 };
 
-template <typename T> int run_col(ptf_handle* h, const ColGeom& g, int mode, const ColIO& io, bool do_inverse) {
+// Solves [b0, b0 + nb) of the batch: every per-solve field pointer is
+// offset by b0 solves.
+struct Group { int b0 = 0, nb = 0; cudaStream_t st = nullptr; };
+
+template <typename C> C* goff(const void* p, const ptf_handle* h, const Group& gr) {
+  return p ? (C*)p + (size_t)gr.b0 * (size_t)h->plane : nullptr;
+}
+
+template <typename T> int run_col(ptf_handle* h, const ColGeom& g, int mode, const ColIO& io, bool do_inverse,
+                                  Group gr = Group()) {
   typedef typename cplx_of<T>::type C;
+  if (gr.nb == 0) gr.nb = h->cfg.batch;
   ColArgs<T> a;
   std::memset(&a, 0, sizeof(a));
-  a.nxin = (const C*)io.nxin;
-  a.s = (C*)(io.s ? io.s : h->s);
-  a.si = (C*)h->si; a.acc = (C*)h->acc; a.n1 = (C*)h->n1;
-  a.A = (C*)io.A; a.B = (C*)io.B; a.Cout = (C*)io.Cout; a.z2in = (const C*)io.z2in; a.nout = (C*)io.nout;
+  a.nxin = goff<const C>(io.nxin, h, gr);
+  a.s = goff<C>(io.s ? io.s : h->s, h, gr);
+  a.si = goff<C>(h->si, h, gr); a.acc = goff<C>(h->acc, h, gr); a.n1 = goff<C>(h->n1, h, gr);
+  a.A = goff<C>(io.A, h, gr); a.B = goff<C>(io.B, h, gr); a.Cout = goff<C>(io.Cout, h, gr);
+  a.z2in = goff<const C>(io.z2in, h, gr); a.nout = goff<C>(io.nout, h, gr);
   a.tw = (const C*)(g.axis == 2 ? h->twz : h->twy);
   a.Ltab = (const T*)h->Ltab; a.coef = (const T*)h->coef;
   a.dt = (T)h->cfg.dt;
   a.dk = (T)g.dk;
   a.stride = g.stride; a.mode = mode; a.do_inverse = do_inverse ? 1 : 0;
   a.bstride = g.bstride; a.tplane = h->plane; a.tab_per_block = 0;
+  if (h->k0mode && &g == &h->gmain) {
+    a.k0 = h->k0 + 4 * (size_t)gr.b0;
+    a.k0c = h->k0c;
+    a.dt64 = h->cfg.dt;
+  }
+  const int nblk_y = (int)((long long)g.nblk_y * gr.nb / h->cfg.batch);  // blocks of fields of the group
+  cudaStream_t st = gr.st ? gr.st : h->stream;
   cudaEvent_t e0;
-  prof_begin(h, &e0);
-  cudaError_t e = launch_col<T>(g.n, a, g.W, g.ncols / g.W, g.nblk_y, h->stream);
-  prof_end(h, e0, 0, pass_bytes(h, 0, mode));
+  prof_begin(h, &e0, st);
+  cudaError_t e = launch_col<T>(g.n, a, g.W, g.ncols / g.W, nblk_y, st);
+  prof_end(h, e0, 0, pass_bytes(h, 0, mode) * gr.nb / h->cfg.batch, st);
   h->launches++;
   if (e != cudaSuccess) return cuda_fail(h, e, "column pass launch");
   return PTF_OK;
@@ -331,25 +380,31 @@ template <typename T> int run_col(ptf_handle* h, const ColGeom& g, int mode, con
 
 template <typename T>
 int run_row(ptf_handle* h, int mode, const void* A, const void* B, const void* Cin, void* out, const void* cin,
-            void* cout, double scale) {
+            void* cout, double scale, Group gr = Group()) {
   typedef typename cplx_of<T>::type C;
+  if (gr.nb == 0) gr.nb = h->cfg.batch;
   RowArgs<T> a;
   std::memset(&a, 0, sizeof(a));
-  a.A = (const C*)A; a.B = (const C*)B; a.Cin = (const C*)Cin; a.out = (C*)out;
+  a.A = goff<const C>(A, h, gr); a.B = goff<const C>(B, h, gr); a.Cin = goff<const C>(Cin, h, gr);
+  a.out = goff<C>(out, h, gr);
   a.u = (const T*)h->u; a.v = (const T*)h->v; a.w = (const T*)h->w;
-  a.cin = (const T*)cin; a.cout = (T*)cout;
+  a.cin = cin ? (const T*)cin + (size_t)gr.b0 * h->nphys : nullptr;
+  a.cout = cout ? (T*)cout + (size_t)gr.b0 * h->nphys : nullptr;
   a.tw = (const C*)h->twx;
   a.dkx = (T)(2 * M_PI / h->cfg.Lx);
   a.scale = (T)scale;
   a.rows = (int)h->rows; a.pitch = h->pitch; a.mode = mode;
   a.park_slots = h->dim == 3 ? 2 : 1;
+  a.err = h->err_dev;
+  a.tma = (h->row_tma && h->dim == 2 && mode == ROW_RHS) ? 1 : 0;
   a.bstride = h->plane; a.pstride = h->nphys; a.fstride = 0;
   const int P = h->rowP;
   const int nby = (int)((h->rows / 2) / P);
+  cudaStream_t st = gr.st ? gr.st : h->stream;
   cudaEvent_t e0;
-  prof_begin(h, &e0);
-  cudaError_t e = launch_row<T>(h->nx, a, P, nby, h->cfg.batch, h->stream);
-  prof_end(h, e0, 1, pass_bytes(h, 1, mode));
+  prof_begin(h, &e0, st);
+  cudaError_t e = launch_row<T>(h->nx, a, P, nby, gr.nb, st);
+  prof_end(h, e0, 1, pass_bytes(h, 1, mode) * gr.nb / h->cfg.batch, st);
   h->launches++;
   if (e != cudaSuccess) return cuda_fail(h, e, "row pass launch");
   return PTF_OK;
@@ -379,36 +434,134 @@ template <typename T> int do_prologue(ptf_handle* h, void* sbuf = nullptr) {
 
 // One RHS evaluation up to and including the main column pass, whose mode
 // (a stage combination, or a plain forward into nout) the caller picks.
-template <typename T> int rhs_and_column(ptf_handle* h, int col_mode, void* nout, bool do_inverse) {
+template <typename T> int rhs_and_column(ptf_handle* h, int col_mode, void* nout, bool do_inverse,
+                                         Group gr = Group()) {
   int rc;
   if (h->dim == 2) {
-    rc = run_row<T>(h, ROW_RHS, h->A, h->B, nullptr, h->Nx, nullptr, nullptr, 1.0);
+    rc = run_row<T>(h, ROW_RHS, h->A, h->B, nullptr, h->Nx, nullptr, nullptr, 1.0, gr);
     if (rc) return rc;
     ColIO io;
     io.nxin = h->Nx; io.A = h->A; io.B = h->B; io.nout = nout;
-    return run_col<T>(h, h->gmain, col_mode, io, do_inverse);
+    return run_col<T>(h, h->gmain, col_mode, io, do_inverse, gr);
   }
-  rc = run_row<T>(h, ROW_RHS3, h->A, h->B, h->C, h->A, nullptr, nullptr, 1.0);
+  rc = run_row<T>(h, ROW_RHS3, h->A, h->B, h->C, h->A, nullptr, nullptr, 1.0, gr);
   if (rc) return rc;
   ColIO yf;
   yf.nxin = h->A; yf.nout = h->A;
-  rc = run_col<T>(h, h->gy3, COL_FWD_N, yf, false);
+  rc = run_col<T>(h, h->gy3, COL_FWD_N, yf, false, gr);
   if (rc) return rc;
   ColIO z;
   z.nxin = h->A; z.A = h->A; z.B = h->C; z.nout = nout;
-  rc = run_col<T>(h, h->gmain, col_mode, z, do_inverse);
+  rc = run_col<T>(h, h->gmain, col_mode, z, do_inverse, gr);
   if (rc || !do_inverse) return rc;
   ColIO y;
   y.s = h->A; y.z2in = h->C; y.A = h->A; y.B = h->B; y.Cout = h->C;
-  return run_col<T>(h, h->gy3, COL_YINV3, y, true);
+  return run_col<T>(h, h->gy3, COL_YINV3, y, true, gr);
+}
+
+// Solves per group: as many as keep a group's per-solve fields within about
+// 3/4 of L2 (shared tables and flow take the rest), at least one.
+int auto_group(const ptf_handle* h) {
+  int dev = 0, l2 = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+  const double per = 7.0 * (double)h->plane * (double)elem_c(h);
+  const double shared = (double)h->plane * elem_r(h) * (h->cfg.stepper == PTF_ETDRK4 ? 7 : 1) +
+                        (double)h->nphys * elem_r(h) * h->dim;
+  int g = (int)((0.75 * (double)l2 - shared) / per);
+  (void)g;
+  // Measured on GB300 (16 x 1024^2, FP32): the passes are latency bound and
+  // lose more to smaller launches than they gain from L2 residency, so the
+  // default is the whole batch per launch; ptf_set_schedule picks groups.
+  return (int)h->cfg.batch;
+}
+
+// One step: the four stages of every group.  Groups are dealt round-robin to
+// `branches` streams (the handle's stream and up to three side streams that
+// fork from it and join back), so passes of different groups can run at the
+// same time; within a branch the groups follow one another.
+template <typename T> int enqueue_step(ptf_handle* h, int group) {
+  const bool etd = h->cfg.stepper == PTF_ETDRK4;
+  const int nbr = std::max(1, std::min(h->branches, 4));
+  if (nbr > 1) {
+    for (int k = 0; k < nbr - 1; ++k) {
+      if (!h->side[k]) {
+        cudaError_t e = cudaStreamCreateWithFlags(&h->side[k], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join[k], cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_fail(h, e, "side stream");
+      }
+    }
+    if (!h->ev_fork) {
+      cudaError_t e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+      if (e != cudaSuccess) return cuda_fail(h, e, "fork event");
+    }
+    cudaEventRecord(h->ev_fork, h->stream);
+    for (int k = 0; k < nbr - 1; ++k) cudaStreamWaitEvent(h->side[k], h->ev_fork, 0);
+  }
+  int gi = 0;
+  for (int b0 = 0; b0 < h->cfg.batch; b0 += group, ++gi) {
+    Group gr;
+    gr.b0 = b0;
+    gr.nb = std::min(group, h->cfg.batch - b0);
+    const int br = gi % nbr;
+    gr.st = br == 0 ? h->stream : h->side[br - 1];
+    for (int st = 0; st < 4; ++st) {
+      int rc = rhs_and_column<T>(h, (etd ? COL_ETD_1 : COL_RK4_1) + st, nullptr, true, gr);
+      if (rc) return rc;
+    }
+  }
+  if (nbr > 1) {
+    for (int k = 0; k < nbr - 1; ++k) {
+      cudaEventRecord(h->ev_join[k], h->side[k]);
+      cudaStreamWaitEvent(h->stream, h->ev_join[k], 0);
+    }
+  }
+  return PTF_OK;
+}
+
+void drop_graph(ptf_handle* h);
+void drop_graph(ptf_handle* h) {
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  if (h->graph) cudaGraphDestroy(h->graph);
+  h->gexec = nullptr;
+  h->graph = nullptr;
+  h->graph_group = -1;
 }
 
 template <typename T> int do_steps(ptf_handle* h, long long nsteps) {
   if (!h->ab_valid) { int rc = do_prologue<T>(h); if (rc) return rc; }
-  const bool etd = h->cfg.stepper == PTF_ETDRK4;
+  int group = h->group > 0 ? std::min(h->group, (int)h->cfg.batch) : auto_group(h);
+  if (h->branches > 1 && h->group == 0) group = (h->cfg.batch + h->branches - 1) / h->branches;
+  // Replay a captured step unless per-pass timing is on (it records events
+  // between the launches).
+  bool graph = h->use_graph && !h->profiling && nsteps > 1;
+  if (graph && (!h->gexec || h->graph_group != group)) {
+    drop_graph(h);
+    cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(h, e, "graph capture");
+    const long long l0 = h->launches;
+    const int rc = enqueue_step<T>(h, group);
+    e = cudaStreamEndCapture(h->stream, &h->graph);
+    h->launches = l0;
+    if (rc == PTF_OK && e == cudaSuccess) e = cudaGraphInstantiate(&h->gexec, h->graph, 0);
+    if (rc != PTF_OK || e != cudaSuccess) {
+      // capture is an optimisation only: step with direct launches instead
+      drop_graph(h);
+      cudaGetLastError();
+      h->use_graph = 0;
+      graph = false;
+    } else {
+      h->graph_group = group;
+    }
+  }
+  const int per_step = (int)(((h->cfg.batch + group - 1) / group) * 4 * (h->dim == 3 ? 4 : 2));
   for (long long n = 0; n < nsteps; ++n) {
-    for (int st = 0; st < 4; ++st) {
-      int rc = rhs_and_column<T>(h, (etd ? COL_ETD_1 : COL_RK4_1) + st, nullptr, true);
+    if (graph) {
+      cudaError_t e = cudaGraphLaunch(h->gexec, h->stream);
+      if (e != cudaSuccess) return cuda_fail(h, e, "graph launch");
+      h->launches += per_step;
+    } else {
+      int rc = enqueue_step<T>(h, group);
       if (rc) return rc;
     }
     h->t += h->cfg.dt;
@@ -436,9 +589,20 @@ template <typename T> int phys_in(ptf_handle* h, const double* src, int where, T
   return PTF_OK;
 }
 
+// FP64 k = 0 mode scratch: sum partials and per-solve sums
+double* k0_partials(const ptf_handle* h) { return h->k0 + 4 * (size_t)h->cfg.batch; }
+double* k0_sums(const ptf_handle* h) { return h->k0 + 68 * (size_t)h->cfg.batch; }
+
 template <typename T> int set_c_impl(ptf_handle* h, const double* c, int where) {
   int rc = phys_in<T>(h, c, where, (T*)h->phys, h->nphys * h->cfg.batch, 1.0);
   if (rc) return rc;
+  if (h->k0mode) {
+    // s(0,0[,0]) = sum of c, compensated, from the FP64 input
+    const double* dsrc = where == PTF_HOST ? h->stage : c;
+    cudaError_t e = launch_solve_sums<double>(dsrc, h->nphys, h->cfg.batch, k0_partials(h), h->k0, 4, h->stream);
+    h->launches += 2;
+    if (e != cudaSuccess) return cuda_fail(h, e, "k = 0 mode sum");
+  }
   void* nx = h->dim == 2 ? h->Nx : h->A;
   rc = run_row<T>(h, ROW_R2C, nullptr, nullptr, nullptr, nx, h->phys, nullptr, 0.5);
   if (rc) return rc;
@@ -467,8 +631,17 @@ template <typename T> int get_c_impl(ptf_handle* h, double* dst) {
   rc = run_row<T>(h, ROW_C2R, h->A, nullptr, nullptr, nullptr, nullptr, h->phys, inv);
   if (rc) return rc;
   const long long n = h->nphys * h->cfg.batch;
-  cudaError_t e = launch_real_out<T>((const T*)h->phys, dst, n, h->stream);
-  h->launches++;
+  cudaError_t e;
+  if (h->k0mode) {
+    // shift each solve's field so that its sum is the FP64 (0,0[,0]) mode
+    e = launch_solve_sums<T>((const T*)h->phys, h->nphys, h->cfg.batch, k0_partials(h), k0_sums(h), 1, h->stream);
+    if (e == cudaSuccess)
+      e = launch_real_out_shift<T>((const T*)h->phys, dst, h->nphys, h->cfg.batch, h->k0, k0_sums(h), h->stream);
+    h->launches += 3;
+  } else {
+    e = launch_real_out<T>((const T*)h->phys, dst, n, h->stream);
+    h->launches++;
+  }
   if (e != cudaSuccess) return cuda_fail(h, e, "get_c");
   return PTF_OK;
 }
@@ -502,13 +675,18 @@ int spec_in(ptf_handle* h, const double* sol, int32_t where, void* dst) {
   return PTF_OK;
 }
 
-int spec_out(ptf_handle* h, const void* src, double* user, int32_t where) {
+// k0patch: the (0,0[,0]) element of each solve comes from the FP64 k = 0 state
+int spec_out(ptf_handle* h, const void* src, double* user, int32_t where, bool k0patch = false) {
   const long long rows = h->rows * h->cfg.batch;
   const long long n = rows * h->nkr;
   double2* dst = (where == PTF_HOST) ? (double2*)h->stage : (double2*)user;
   cudaError_t e = h->fp32 ? launch_spec_out<float>((const float2*)src, dst, h->nkr, h->pitch, rows, h->stream)
                           : launch_spec_out<double>((const double2*)src, dst, h->nkr, h->pitch, rows, h->stream);
   h->launches++;
+  if (e == cudaSuccess && k0patch) {
+    e = launch_k0_to_spec(dst, h->rows * h->nkr, h->cfg.batch, h->k0, h->stream);
+    h->launches++;
+  }
   if (e != cudaSuccess) return cuda_fail(h, e, "spectral convert");
   if (where == PTF_HOST) {
     e = cudaMemcpyAsync(user, h->stage, n * sizeof(double2), cudaMemcpyDeviceToHost, h->stream);
@@ -516,6 +694,147 @@ int spec_out(ptf_handle* h, const void* src, double* user, int32_t where) {
     if (e != cudaSuccess) return cuda_fail(h, e, "spectral copy");
   }
   return PTF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Launch-shape tuning.  The shapes (columns per column-pass block, row pairs
+// per row-pass block, stream branches, the row pass's staged variant) change
+// no result, only the time per step, so they are picked by timing whole
+// steps on the handle itself, one knob at a time; the state is saved before
+// and restored after, so tuning leaves the solve where it was.  Choices are
+// cached per (precision, grid, batch, stepper) for the process.
+// ---------------------------------------------------------------------------
+std::mutex g_tune_mutex;
+std::map<std::string, ptf_tuning> g_tune_cache;
+
+std::string tuning_key(const ptf_handle* h) {
+  char buf[160];
+  std::snprintf(buf, sizeof(buf), "%d:%d:%d:%d:%d:%d:%d:%d", h->fp32 ? 32 : 64, h->dim, h->nx, h->ny, h->nz,
+                (int)h->cfg.batch, (int)h->cfg.stepper, h->k0mode ? 1 : 0);
+  return buf;
+}
+
+ptf_tuning current_tuning(const ptf_handle* h) {
+  ptf_tuning t;
+  std::memset(&t, 0, sizeof(t));
+  t.col_lines = h->gmain.W;
+  t.col_lines_y = h->dim == 3 ? h->gy3.W : 0;
+  t.row_pairs = h->rowP;
+  t.branches = h->branches;
+  t.solves_per_group = h->group;
+  t.row_staged = h->row_tma;
+  t.ms_per_step = h->tuned_ms;
+  return t;
+}
+
+bool lines_ok(const ptf_handle* h, int n, bool col, int W, long long divisor) {
+  if (W < 1 || (W & (W - 1)) || divisor % W) return false;
+  const int mx = h->fp32 ? max_lines_per_block<float>(n, col) : max_lines_per_block<double>(n, col);
+  return W <= mx;
+}
+
+int apply_tuning(ptf_handle* h, const ptf_tuning& t) {
+  if (!lines_ok(h, h->gmain.n, true, t.col_lines, h->gmain.ncols))
+    return fail(h, PTF_ERR_ARG, "col_lines: a power of two dividing the columns, within the block limit");
+  if (h->dim == 3 && !lines_ok(h, h->gy3.n, true, t.col_lines_y, h->gy3.ncols))
+    return fail(h, PTF_ERR_ARG, "col_lines_y: a power of two dividing the columns, within the block limit");
+  if (!lines_ok(h, h->nx, false, t.row_pairs, h->rows / 2))
+    return fail(h, PTF_ERR_ARG, "row_pairs: a power of two dividing the row pairs, within the block limit");
+  if (t.branches < 1 || t.branches > 4) return fail(h, PTF_ERR_ARG, "branches must be 1..4");
+  if (t.solves_per_group < 0) return fail(h, PTF_ERR_ARG, "solves_per_group must be >= 0");
+  if (t.row_staged != 0 && t.row_staged != 1) return fail(h, PTF_ERR_ARG, "row_staged must be 0 or 1");
+  h->gmain.W = t.col_lines;
+  if (h->dim == 3) h->gy3.W = t.col_lines_y;
+  h->rowP = t.row_pairs;
+  h->branches = t.branches;
+  h->group = t.solves_per_group;
+  h->row_tma = h->dim == 2 ? t.row_staged : 0;
+  h->tuned_ms = t.ms_per_step;
+  drop_graph(h);
+  return PTF_OK;
+}
+
+// Device time of `steps` steps (best of two runs, after one untimed step).
+template <typename T> int time_steps(ptf_handle* h, int steps, double* ms) {
+  int rc = do_steps<T>(h, 1);
+  if (rc) return rc;
+  cudaEvent_t a = pool_event(h), b = pool_event(h);
+  double best = 1e30;
+  for (int rep = 0; rep < 2 && !rc; ++rep) {
+    cudaEventRecord(a, h->stream);
+    if ((rc = do_steps<T>(h, steps))) break;
+    cudaEventRecord(b, h->stream);
+    cudaError_t e = cudaEventSynchronize(b);
+    float t = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+    if (e != cudaSuccess) rc = cuda_fail(h, e, "tuning timer");
+    else best = std::min(best, (double)t / steps);
+  }
+  h->event_pool.push_back(a);
+  h->event_pool.push_back(b);
+  *ms = best;
+  return rc;
+}
+
+template <typename T> int autotune_impl(ptf_handle* h, int steps) {
+  typedef typename cplx_of<T>::type C;
+  const size_t sbytes = (size_t)h->plane * h->cfg.batch * sizeof(C);
+  void* saved = nullptr;
+  double* saved_k0 = nullptr;
+  if (cudaMalloc(&saved, sbytes) != cudaSuccess) { cudaGetLastError(); return fail(h, PTF_ERR_MEMORY, "tuning: state copy"); }
+  if (h->k0mode && cudaMalloc((void**)&saved_k0, 4 * sizeof(double) * h->cfg.batch) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(saved);
+    return fail(h, PTF_ERR_MEMORY, "tuning: state copy");
+  }
+  const double t0 = h->t;
+  const long long step0 = h->step;
+  cudaError_t e = cudaMemcpyAsync(saved, h->s, sbytes, cudaMemcpyDeviceToDevice, h->stream);
+  if (e == cudaSuccess && saved_k0)
+    e = cudaMemcpyAsync(saved_k0, h->k0, 4 * sizeof(double) * h->cfg.batch, cudaMemcpyDeviceToDevice, h->stream);
+  int rc = e == cudaSuccess ? PTF_OK : cuda_fail(h, e, "tuning: save state");
+
+  ptf_tuning best = current_tuning(h);
+  double best_ms = 1e30;
+  auto trial = [&](const ptf_tuning& t) -> int {
+    int r = apply_tuning(h, t);
+    if (r) return r;
+    double ms = 0;
+    if ((r = time_steps<T>(h, steps, &ms))) return r;
+    if (ms < best_ms) { best_ms = ms; best = t; best.ms_per_step = ms; }
+    return PTF_OK;
+  };
+  if (!rc) rc = trial(best);
+  // one knob at a time, starting from the best so far
+  for (int knob = 0; knob < 5 && !rc; ++knob) {
+    std::vector<ptf_tuning> cands;
+    for (int v = 1; v <= 64; v *= 2) {
+      ptf_tuning t = best;
+      if (knob == 0) { if (!lines_ok(h, h->gmain.n, true, v, h->gmain.ncols)) continue; t.col_lines = v; }
+      else if (knob == 1) { if (h->dim != 3 || !lines_ok(h, h->gy3.n, true, v, h->gy3.ncols)) continue; t.col_lines_y = v; }
+      else if (knob == 2) { if (!lines_ok(h, h->nx, false, v, h->rows / 2)) continue; t.row_pairs = v; }
+      else if (knob == 3) { if (v > 4 || v > h->cfg.batch) continue; t.branches = v; t.solves_per_group = 0; }
+      else { if (v > 2 || h->dim != 2) continue; t.row_staged = v - 1; }
+      cands.push_back(t);
+    }
+    for (const ptf_tuning& t : cands) {
+      if (std::memcmp(&t, &best, offsetof(ptf_tuning, ms_per_step)) == 0) continue;
+      if ((rc = trial(t))) break;
+    }
+  }
+  if (!rc) rc = apply_tuning(h, best);
+  // restore the solve
+  e = cudaMemcpyAsync(h->s, saved, sbytes, cudaMemcpyDeviceToDevice, h->stream);
+  if (e == cudaSuccess && saved_k0)
+    e = cudaMemcpyAsync(h->k0, saved_k0, 4 * sizeof(double) * h->cfg.batch, cudaMemcpyDeviceToDevice, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(saved);
+  if (saved_k0) cudaFree(saved_k0);
+  if (e != cudaSuccess && !rc) rc = cuda_fail(h, e, "tuning: restore state");
+  h->t = t0;
+  h->step = step0;
+  h->ab_valid = false;
+  return rc;
 }
 
 }  // namespace
@@ -541,6 +860,7 @@ void ptf_config_default(ptf_config* c, int32_t dim) {
   c->precision = PTF_FP64;
   c->time_mode = PTF_CLOCK_T;
   c->batch = 1;
+  c->k0_mode = 1;
 }
 
 const char* ptf_last_error(const ptf_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
@@ -548,6 +868,12 @@ const char* ptf_last_error(const ptf_handle* h) { return h ? h->err.c_str() : g_
 void ptf_destroy(ptf_handle* h) {
   if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
+  drop_graph(h);
+  for (int k = 0; k < 3; ++k) {
+    if (h->side[k]) { cudaStreamSynchronize(h->side[k]); cudaStreamDestroy(h->side[k]); }
+    if (h->ev_join[k]) cudaEventDestroy(h->ev_join[k]);
+  }
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   prof_clear(h);
   for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
   for (void* p : h->allocs) cudaFree(p);
@@ -572,6 +898,7 @@ int ptf_create(const ptf_config* cfg, ptf_handle** out) {
   if (c.time_mode != PTF_CLOCK_T && c.time_mode != PTF_STAGE_T) return fail(nullptr, PTF_ERR_ARG, "time_mode must be CLOCK_T or STAGE_T");
   if (c.batch < 1) return fail(nullptr, PTF_ERR_ARG, "batch must be >= 1");
   if (c.nkappah < 0) return fail(nullptr, PTF_ERR_ARG, "nkappah must be >= 0");
+  if (c.k0_mode != 0 && c.k0_mode != 1) return fail(nullptr, PTF_ERR_ARG, "k0_mode must be 0 or 1");
   if (!std::isfinite(c.kappa) || !std::isfinite(c.eta) || !std::isfinite(c.iota) || !std::isfinite(c.kappah))
     return fail(nullptr, PTF_ERR_ARG, "diffusivities must be finite");
 
@@ -580,6 +907,7 @@ int ptf_create(const ptf_config* cfg, ptf_handle** out) {
   h->dim = c.dim;
   h->nx = c.nx; h->ny = c.ny; h->nz = c.dim == 3 ? c.nz : 1;
   h->fp32 = c.precision == PTF_FP32;
+  h->k0mode = h->fp32 && c.k0_mode == 1;
   h->nkr = c.nx / 2 + 1;
   h->pitch = ((h->nkr + 7) / 8) * 8;
   h->plane = (long long)h->nz * h->ny * h->pitch;
@@ -605,6 +933,8 @@ int ptf_create(const ptf_config* cfg, ptf_handle** out) {
     y.bstride = (long long)h->ny * h->pitch; y.dk = 2 * M_PI / c.Ly; y.axis = 1; y.W = lines(h->ny, true, h->pitch);
   }
   h->rowP = lines(h->nx, false, (int)(h->rows / 2));
+  // two concurrent stream branches for batches (measured +4% on 16 x 1024^2)
+  h->branches = c.batch >= 2 ? 2 : 1;
   const size_t B = (size_t)c.batch;
   const size_t sc = (size_t)h->plane * B * elem_c(h);
   const size_t sp = (size_t)h->nphys * B * elem_r(h);
@@ -623,6 +953,9 @@ int ptf_create(const ptf_config* cfg, ptf_handle** out) {
   ok = ok && dev_alloc(h, &h->phys, sp);
   h->stage_elems = std::max<long long>(h->nphys * (long long)B, 2 * h->rows * h->nkr * (long long)B);
   ok = ok && dev_alloc(h, (void**)&h->stage, (size_t)h->stage_elems * sizeof(double));
+  ok = ok && dev_alloc(h, (void**)&h->err_dev, sizeof(int));
+  if (h->k0mode)
+    ok = ok && dev_alloc(h, (void**)&h->k0, 69 * B * sizeof(double)) && dev_alloc(h, (void**)&h->k0c, 8 * sizeof(double));
   if (!ok) {
     const long long held = h->bytes;
     ptf_destroy(h);
@@ -685,7 +1018,7 @@ int ptf_get_sol(ptf_handle* h, double* sol, int32_t where) {
   if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
   if (!sol) return fail(h, PTF_ERR_ARG, "null field");
   if (check_where(h, where)) return PTF_ERR_ARG;
-  return spec_out(h, h->s, sol, where);
+  return spec_out(h, h->s, sol, where, h->k0mode);
 }
 
 int ptf_set_sol(ptf_handle* h, const double* sol, int32_t where) {
@@ -694,6 +1027,12 @@ int ptf_set_sol(ptf_handle* h, const double* sol, int32_t where) {
   if (check_where(h, where)) return PTF_ERR_ARG;
   int rc = spec_in(h, sol, where, h->s);
   if (rc) return rc;
+  if (h->k0mode) {
+    const double2* src = where == PTF_HOST ? (const double2*)h->stage : (const double2*)sol;
+    cudaError_t e = launch_k0_from_spec(src, h->rows * h->nkr, h->cfg.batch, h->k0, h->stream);
+    h->launches++;
+    if (e != cudaSuccess) return cuda_fail(h, e, "k = 0 mode seed");
+  }
   h->ab_valid = false;
   h->have_c = true;
   if (where == PTF_HOST) {
@@ -742,6 +1081,10 @@ int ptf_synchronize(ptf_handle* h) {
   if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
   cudaError_t e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return cuda_fail(h, e, "synchronize");
+  int err = 0;
+  e = cudaMemcpy(&err, h->err_dev, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(h, e, "error flag");
+  if (err) return fail(h, PTF_ERR_CUDA, "a kernel gave up waiting for its bulk copies (bounded wait ran out)");
   return PTF_OK;
 }
 int ptf_get_stream(const ptf_handle* h, void** stream) {
@@ -753,6 +1096,7 @@ int ptf_set_stream(ptf_handle* h, void* stream) {
   if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
   cudaError_t e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return cuda_fail(h, e, "synchronize");
+  drop_graph(h);
   if (h->own_stream) cudaStreamDestroy(h->stream);
   h->own_stream = false;
   h->stream = (cudaStream_t)stream;
@@ -761,6 +1105,19 @@ int ptf_set_stream(ptf_handle* h, void* stream) {
 int ptf_device_bytes(const ptf_handle* h, int64_t* bytes) {
   if (!h || !bytes) return fail(nullptr, PTF_ERR_ARG, "null argument");
   *bytes = h->bytes;
+  return PTF_OK;
+}
+
+int ptf_set_schedule(ptf_handle* h, int32_t solves_per_group, int32_t branches, int32_t use_graph) {
+  if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
+  if (solves_per_group < 0) return fail(h, PTF_ERR_ARG, "solves_per_group must be >= 0 (0: automatic)");
+  if (branches < 1 || branches > 4) return fail(h, PTF_ERR_ARG, "branches must be 1..4");
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return cuda_fail(h, e, "synchronize");
+  h->group = solves_per_group;
+  h->branches = branches;
+  h->use_graph = use_graph ? 1 : 0;
+  drop_graph(h);
   return PTF_OK;
 }
 
@@ -795,6 +1152,37 @@ int ptf_profile_read(ptf_handle* h, int32_t kind, double* total_ms, int64_t* lau
 int ptf_kernel_launches(const ptf_handle* h, int64_t* count) {
   if (!h || !count) return fail(nullptr, PTF_ERR_ARG, "null argument");
   *count = h->launches;
+  return PTF_OK;
+}
+
+int ptf_get_tuning(const ptf_handle* h, ptf_tuning* out) {
+  if (!h || !out) return fail(nullptr, PTF_ERR_ARG, "null argument");
+  *out = current_tuning(h);
+  return PTF_OK;
+}
+
+int ptf_set_tuning(ptf_handle* h, const ptf_tuning* t) {
+  if (!h || !t) return fail(nullptr, PTF_ERR_ARG, "null argument");
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return cuda_fail(h, e, "synchronize");
+  return apply_tuning(h, *t);
+}
+
+int ptf_autotune(ptf_handle* h, int32_t trial_steps, int32_t flags) {
+  if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
+  if (trial_steps < 1 || trial_steps > 1000) return fail(h, PTF_ERR_ARG, "trial_steps must be in 1..1000");
+  if (!h->have_flow) return fail(h, PTF_ERR_STATE, "no flow set (ptf_set_flow_arrays)");
+  if (h->profiling) return fail(h, PTF_ERR_STATE, "per-pass timing is on (ptf_profile)");
+  const std::string key = tuning_key(h);
+  if (!(flags & PTF_TUNE_FORCE)) {
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) return apply_tuning(h, it->second);
+  }
+  const int rc = h->fp32 ? autotune_impl<float>(h, trial_steps) : autotune_impl<double>(h, trial_steps);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(g_tune_mutex);
+  g_tune_cache[key] = current_tuning(h);
   return PTF_OK;
 }
 

@@ -27,4 +27,17 @@ template <typename T> cudaError_t launch_real_out(const T* src, double* dst, lon
 template <typename T> cudaError_t launch_spec_in(const double2* src, typename cplx_of<T>::type* dst, int nkr, int pitch, long long rows, cudaStream_t st);
 template <typename T> cudaError_t launch_spec_out(const typename cplx_of<T>::type* src, double2* dst, int nkr, int pitch, long long rows, cudaStream_t st);
 
+// FP64 k = 0 mode (ptf_util.cu).  Per-solve sums of x (n values per solve):
+// out[b * out_stride]; partials holds 64 doubles per solve.
+template <typename Tin>
+cudaError_t launch_solve_sums(const Tin* x, long long n, int batch, double* partials, double* out, int out_stride,
+                              cudaStream_t st);
+// k0[4b] = Re src[b * per_solve]; dst[b * per_solve] = (k0[4b], 0)
+cudaError_t launch_k0_from_spec(const double2* src, long long per_solve, int batch, double* k0, cudaStream_t st);
+cudaError_t launch_k0_to_spec(double2* dst, long long per_solve, int batch, const double* k0, cudaStream_t st);
+// dst = src + (k0[4b] - sums[b]) / n per solve b
+template <typename T>
+cudaError_t launch_real_out_shift(const T* src, double* dst, long long n, int batch, const double* k0,
+                                  const double* sums, cudaStream_t st);
+
 }  // namespace ptf

@@ -41,6 +41,16 @@ template <typename T, int N> struct PassLaunch {
     }
   }
   static cudaError_t row(const RowArgs<T>& a, int P, int nby, int batch, cudaStream_t st) {
+    // the staged variant when its shared memory fits, else the direct kernel
+    if (a.tma && a.mode == ROW_RHS && row_tma_smem_bytes<T, N>(P, a.pitch) <= 227u * 1024u &&
+        P * pass_tpl<T, N>() <= max_threads(row_rhs_tma_kernel<T, N>)) {
+      const size_t smem = row_tma_smem_bytes<T, N>(P, a.pitch);
+      cudaError_t e = cudaFuncSetAttribute(row_rhs_tma_kernel<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem);
+      if (e != cudaSuccess) return e;
+      row_rhs_tma_kernel<T, N><<<dim3(nby, batch), dim3(P * pass_tpl<T, N>()), smem, st>>>(a);
+      return cudaGetLastError();
+    }
     if (P * pass_tpl<T, N>() > max_threads(row_pass_kernel<T, N>)) return cudaErrorInvalidConfiguration;
     const size_t smem = row_smem_bytes<T, N>(P, a.park_slots < 1 ? 1 : a.park_slots);
     cudaError_t e = cudaFuncSetAttribute(row_pass_kernel<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -22,6 +22,7 @@
 // of the two-for-one separation into the product.
 #pragma once
 #include "ptf_fft.cuh"
+#include "ptf_tma.cuh"
 
 namespace ptf {
 
@@ -80,6 +81,12 @@ template <typename T> struct ColArgs {
   const SlotParams<T>* slots;
   const int* slot_list;
   int nslots, slot_cols;
+  // FP64 k = 0 mode (FP32 handles, main column pass): per-solve FP64 state
+  // {s, stage input, acc, N1} of the (0,0[,0]) mode and its FP64
+  // coefficients {L, E, E2, zeta, alpha, beta, gamma}; null when off
+  double* k0;
+  const double* k0c;
+  double dt64;
 };
 
 template <typename T> struct RowArgs {
@@ -104,7 +111,11 @@ template <typename T> struct RowArgs {
   int nslots;
   T stage_c;       // stage time offset in units of dt (0, 1/2, 1/2, 1 for RK4)
   T fscale;        // analytic flow scale: -1/(2 nx ny)
+  int* err;        // device error flag (bounded waits that ran out)
+  int tma;         // 1: ROW_RHS stages its rows in shared memory with bulk copies
 };
+
+
 
 template <typename T, int N>
 __device__ __forceinline__ T kval(int p, T dk) { return (T)(p < N / 2 ? p : p - N) * dk; }
@@ -122,8 +133,17 @@ __device__ __forceinline__ T kval(int p, T dk) { return (T)(p < N / 2 ? p : p - 
 #ifndef PTF_COL_MINB_F64
 #define PTF_COL_MINB_F64 1
 #endif
+#ifndef PTF_COL_THREADS_F32
+#define PTF_COL_THREADS_F32 256
+#endif
+#ifndef PTF_PREFETCH
+#define PTF_PREFETCH 0
+#endif
 template <typename T> struct ColBounds { static constexpr int threads = 256, blocks = PTF_COL_MINB_F64; };
-template <> struct ColBounds<float> { static constexpr int threads = 256, blocks = PTF_COL_MINB_F32; };
+template <> struct ColBounds<float> { static constexpr int threads = PTF_COL_THREADS_F32, blocks = PTF_COL_MINB_F32; };
+
+// Ask L2 to fetch a line now; the load that follows later finds it there.
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 // Dynamic shared memory of a column-pass block with W lines: the W FFT
 // lines, then a private slot array holding each thread's values between
 // transforms.
@@ -131,6 +151,39 @@ template <typename T, int N> __host__ __device__ constexpr size_t col_smem_bytes
   return (size_t)W * (line_stride(N) + N) * sizeof(typename cplx_of<T>::type);
 }
 template <typename T, int N> __host__ __device__ constexpr int pass_tpl() { return N / PassE<T, N>::value; }
+
+// Compensated FP64 sum of the real parts of column 0 of a column-pass block
+// (lines w = 0: threads t*W, registers v[0..E)), returned in thread 0.  Uses
+// the line buffer of line 0 (before the forward transform touches it).
+template <typename T, typename C, int E, int TPL>
+__device__ __forceinline__ double column0_sum(const C* v, int w, int t, C* line0) {
+  double* part = reinterpret_cast<double*>(line0);  // TPL doubles fit in N complex values
+  if (w == 0) {
+    double s = 0, c = 0;
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const double y = (double)v[i].x - c;
+      const double u = s + y;
+      c = (u - s) - y;
+      s = u;
+    }
+    part[t] = s;
+  }
+  __syncthreads();
+  double tot = 0;
+  if (threadIdx.x < 32) {
+    double c = 0;
+    for (int k = threadIdx.x; k < TPL; k += 32) {
+      const double y = part[k] - c;
+      const double u = tot + y;
+      c = (u - tot) - y;
+      tot = u;
+    }
+    for (int off = 16; off > 0; off /= 2) tot += __shfl_xor_sync(0xffffffffu, tot, off);
+  }
+  __syncthreads();
+  return tot;
+}
 
 // Body of one column-pass block (tile = column tile index, blk = block of
 // fields).  BATCHED: flat columns run over the slots of a bucket, each
@@ -176,13 +229,38 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
   // offset of register i for a first/last stage of radix R
 #define PTF_OFF(R, i) (tb + (((i) / (R)) * TPL + ((i) % (R)) * (N / (R))) * stride)
 
+#if PTF_PREFETCH
+  // The stage combination reads state and tables only after the forward
+  // transform: start fetching them now so the transform hides the latency.
+  if (MODE >= COL_RK4_1 && MODE <= COL_ETD_4) {
+    const bool rk = MODE <= COL_RK4_4;
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const int o = PTF_OFF(RF, i);
+      if (MODE == COL_RK4_1 || MODE == COL_RK4_2 || MODE == COL_RK4_3 || MODE == COL_ETD_1 || MODE == COL_ETD_2)
+        prefetch_l2(a.s + boff + o);
+      if (MODE == COL_RK4_2 || MODE == COL_RK4_3 || MODE == COL_RK4_4 || MODE == COL_ETD_3) prefetch_l2(a.si + boff + o);
+      if (MODE != COL_RK4_1 && MODE != COL_ETD_1) prefetch_l2(a.acc + boff + o);
+      if (MODE == COL_ETD_3) prefetch_l2(a.n1 + boff + o);
+      if (rk && !BATCHED) prefetch_l2(a.Ltab + (size_t)(a.tab_per_block ? (size_t)blk * a.tplane : 0) + o);
+    }
+  }
+#endif
+  constexpr bool K0MODE = (MODE >= COL_RK4_1 && MODE <= COL_ETD_4) || MODE == COL_FWD_STORE;
+  const bool k0blk = !BATCHED && K0MODE && a.k0 != nullptr && tile == 0;  // uniform across the block
+  double k0N = 0;
   C v[E];
   if (MODE != COL_PROLOGUE && MODE != COL_YINV3) {
     const C* __restrict__ src = a.nxin + boff;
 #pragma unroll
     for (int i = 0; i < E; ++i) v[i] = src[PTF_OFF(RF0, i)];
+    // FP64 k = 0 mode: N(0,0) is the sum of column 0 (the kr = 0 bins of
+    // the rows, real), taken here as a compensated FP64 sum instead of from
+    // the FP32 transform; it lands in thread 0, which owns position 0.
+    if (k0blk && MODE != COL_FWD_STORE) k0N = column0_sum<T, C, E, TPL>(v, w, t, sm);
     fft_line<N, -1, E>(v, t, line, a.tw);
   }
+  const bool k0thr = k0blk && threadIdx.x == 0;  // column 0, t = 0: position p = 0 is its register 0
 
   // Stage combination at the positions p = reg_pos<N, RF, E>(t, i); the
   // next stage input is parked (each thread reads back only its own slots,
@@ -270,6 +348,35 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
         const C ac = AC[o];
         x.x = ac.x + ga * Nh.x; x.y = ac.y + ga * Nh.y;
         S[o] = x;
+      }
+      if (k0thr && i == 0) {
+        // the (0,0) mode in FP64: {s, stage input, acc, N1} of this solve
+        double* q = a.k0 + (size_t)blk * 4;
+        const double* kc = a.k0c;
+        const double dd = a.dt64, Nd = k0N;
+        double xd = q[0];
+        if (MODE == COL_FWD_STORE) {
+          xd = q[0];
+        } else if (MODE == COL_RK4_1) {
+          const double k = kc[0] * q[0] + Nd;
+          q[2] = q[0] + dd / 6 * k; xd = q[0] + dd / 2 * k; q[1] = xd;
+        } else if (MODE == COL_RK4_2 || MODE == COL_RK4_3) {
+          const double k = kc[0] * q[1] + Nd;
+          q[2] += dd / 3 * k; xd = q[0] + (MODE == COL_RK4_2 ? dd / 2 : dd) * k; q[1] = xd;
+        } else if (MODE == COL_RK4_4) {
+          const double k = kc[0] * q[1] + Nd;
+          xd = q[2] + dd / 6 * k; q[0] = xd;
+        } else if (MODE == COL_ETD_1) {
+          q[3] = Nd; q[2] = kc[1] * q[0] + kc[4] * Nd; xd = kc[2] * q[0] + kc[3] * Nd; q[1] = xd;
+        } else if (MODE == COL_ETD_2) {
+          q[2] += 2 * kc[5] * Nd; xd = kc[2] * q[0] + kc[3] * Nd;
+        } else if (MODE == COL_ETD_3) {
+          q[2] += 2 * kc[5] * Nd; xd = kc[2] * q[1] + kc[3] * (2 * Nd - q[3]);
+        } else {  // COL_ETD_4
+          xd = q[2] + kc[6] * Nd; q[0] = xd;
+        }
+        x.x = (T)xd; x.y = 0;
+        if (MODE == COL_FWD_STORE || MODE == COL_RK4_4 || MODE == COL_ETD_4) S[o] = x;
       }
       park[i * nthr + threadIdx.x] = x;
     }
@@ -466,6 +573,25 @@ __device__ __forceinline__ void row_body(const RowArgs<T>& a, int tile, int blk,
   const long long r0 = boff + (long long)yy0 * pitch, r1 = r0 + pitch;
   const long long q0 = (long long)yy0 * NX, q1 = q0 + NX;
 
+#if PTF_PREFETCH
+  // The flow rows and the second row's inputs are read after the first
+  // inverse transform: start fetching them now.
+  if (a.mode == ROW_RHS || a.mode == ROW_RHS3) {
+    const bool arrays = !BATCHED || a.slots[slot].flow_kind == FLOW_ARRAYS;
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const int x = reg_pos<NX, RIL, E>(t, i);
+      if (arrays) {
+        prefetch_l2(a.u + foff + q0 + x); prefetch_l2(a.v + foff + q0 + x);
+        prefetch_l2(a.u + foff + q1 + x); prefetch_l2(a.v + foff + q1 + x);
+      }
+      const int k = reg_pos<NX, RI0, E>(t, i);
+      const int kk = k <= NX / 2 ? k : NX - k;
+      prefetch_l2(a.A + r1 + kk); prefetch_l2(a.B + r1 + kk);
+    }
+  }
+#endif
+
   C v[E];
   if (a.mode == ROW_R2C) {
 #pragma unroll
@@ -569,6 +695,121 @@ __device__ __forceinline__ void row_body(const RowArgs<T>& a, int tile, int blk,
       a.out[r0 + k] = o0;
       a.out[r1 + k] = o1;
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Row pass, 2D RHS, with bulk-copy staging.  At block start one thread issues
+// bulk copies (cp.async.bulk) of every row the block needs -- A, B of both
+// rows and u, v of both rows, for each of its P pairs -- into shared memory,
+// completing on one mbarrier; the transforms then read their inputs from
+// shared memory.  Per pair: the line, one parking slot array, 4 spectral rows
+// of `pitch` complex values, 4 flow rows of NX reals.
+// ---------------------------------------------------------------------------
+template <typename T, int NX> __host__ __device__ constexpr size_t row_tma_smem_bytes(int P, int pitch) {
+  return (size_t)P * (line_stride(NX) + NX + 4 * pitch) * sizeof(typename cplx_of<T>::type) +
+         (size_t)P * 4 * NX * sizeof(T) + 16;
+}
+
+template <typename T, int NX>
+__global__ void __launch_bounds__(256) row_rhs_tma_kernel(RowArgs<T> a) {
+  typedef typename cplx_of<T>::type C;
+  constexpr int E = PassE<T, NX>::value;
+  constexpr int TPL = NX / E;
+  constexpr int LS = line_stride(NX);
+  constexpr int RI0 = FirstRadix<NX, +1, E>::value;
+  constexpr int RIL = LastRadix<NX, +1, E>::value;
+  constexpr int RFL = LastRadix<NX, -1, E>::value;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* sm = reinterpret_cast<C*>(smem_raw);
+  const int P = blockDim.x / TPL;
+  const int pr = threadIdx.x / TPL, t = threadIdx.x % TPL;
+  const int pitch = a.pitch;
+  C* line = sm + pr * LS;
+  C* park = sm + P * LS + pr * NX;
+  C* rows = sm + P * (LS + NX) + pr * 4 * pitch;  // A0, A1, B0, B1
+  T* flows = reinterpret_cast<T*>(sm + P * (LS + NX + 4 * pitch)) + pr * 4 * NX;  // u0, u1, v0, v1
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + row_tma_smem_bytes<T, NX>(P, pitch) - 16);
+  const long long boff = (long long)blockIdx.y * a.bstride;
+  const long long foff = (long long)blockIdx.y * a.fstride;
+  const int y0 = 2 * (blockIdx.x * P + pr);
+
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t rb = (uint32_t)((((NX / 2 + 1) * sizeof(C)) + 15) / 16 * 16);
+    const uint32_t fb = (uint32_t)(NX * sizeof(T));
+    mbar_arrive_expect_tx(bar, (uint32_t)P * 4u * (rb + fb));
+    for (int q = 0; q < P; ++q) {
+      const int yq = 2 * (blockIdx.x * P + q);
+      C* rq = sm + P * (LS + NX) + q * 4 * pitch;
+      T* fq = reinterpret_cast<T*>(sm + P * (LS + NX + 4 * pitch)) + q * 4 * NX;
+      const C* A0 = a.A + boff + (long long)yq * pitch;
+      const C* B0 = a.B + boff + (long long)yq * pitch;
+      tma_load_1d(rq, A0, rb, bar);
+      tma_load_1d(rq + pitch, A0 + pitch, rb, bar);
+      tma_load_1d(rq + 2 * pitch, B0, rb, bar);
+      tma_load_1d(rq + 3 * pitch, B0 + pitch, rb, bar);
+      const T* u0 = a.u + foff + (long long)yq * NX;
+      const T* v0 = a.v + foff + (long long)yq * NX;
+      tma_load_1d(fq, u0, fb, bar);
+      tma_load_1d(fq + NX, u0 + NX, fb, bar);
+      tma_load_1d(fq + 2 * NX, v0, fb, bar);
+      tma_load_1d(fq + 3 * NX, v0 + NX, fb, bar);
+    }
+  }
+  const bool ok = mbar_wait_bounded(bar, 0, a.err);
+  if (!__syncthreads_and(ok)) return;  // uniform: every thread returns
+
+  const C* A0 = rows;
+  const C* A1 = rows + pitch;
+  const C* B0 = rows + 2 * pitch;
+  const C* B1 = rows + 3 * pitch;
+  const T* u0 = flows;
+  const T* u1 = flows + NX;
+  const T* v0 = flows + 2 * NX;
+  const T* v1 = flows + 3 * NX;
+  C v[E];
+#pragma unroll
+  for (int i = 0; i < E; ++i) v[i] = zsrc_rhs<T, C>(A0, B0, reg_pos<NX, RI0, E>(t, i), NX, a.dkx);
+  fft_line<NX, +1, E>(v, t, line, a.tw);
+#pragma unroll
+  for (int i = 0; i < E; ++i) {
+    const int x = reg_pos<NX, RIL, E>(t, i);
+    C pk; pk.x = u0[x] * v[i].x + v0[x] * v[i].y; pk.y = 0;
+    park[i * TPL + t] = pk;
+  }
+  asm volatile("" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < E; ++i) v[i] = zsrc_rhs<T, C>(A1, B1, reg_pos<NX, RI0, E>(t, i), NX, a.dkx);
+  fft_line<NX, +1, E>(v, t, line, a.tw);
+#pragma unroll
+  for (int i = 0; i < E; ++i) {
+    const int x = reg_pos<NX, RIL, E>(t, i);
+    C w;
+    w.x = park[i * TPL + t].x;
+    w.y = u1[x] * v[i].x + v1[x] * v[i].y;
+    v[i] = w;
+  }
+  fft_line<NX, -1, E>(v, t, line, a.tw);
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < E; ++i) line[smem_pad(reg_pos<NX, RFL, E>(t, i))] = v[i];
+  __syncthreads();
+  const T sc = a.scale;
+  C* out0 = a.out + boff + (long long)y0 * pitch;
+  C* out1 = out0 + pitch;
+  for (int k = t; k <= NX / 2; k += TPL) {
+    const C wk = line[smem_pad(k)];
+    const C wn = line[smem_pad((NX - k) & (NX - 1))];
+    C o0, o1;
+    o0.x = (wk.x + wn.x) * sc; o0.y = (wk.y - wn.y) * sc;
+    o1.x = (wk.y + wn.y) * sc; o1.y = (wn.x - wk.x) * sc;
+    out0[k] = o0;
+    out1[k] = o1;
   }
 }
 

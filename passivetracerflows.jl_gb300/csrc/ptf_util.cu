@@ -64,6 +64,103 @@ cudaError_t launch_spec_out(const typename cplx_of<T>::type* src, double2* dst, 
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// FP64 k = 0 mode helpers.  Per-solve sums run as kSumBlocks blocks per solve
+// writing FP64 partials, then one warp per solve adding the partials with a
+// compensated (Kahan) sum.  FP64 inputs also use compensated per-thread sums;
+// FP32 values are exact in FP64, so a plain FP64 accumulation suffices.
+// ---------------------------------------------------------------------------
+constexpr int kSumBlocks = 64;
+
+__device__ __forceinline__ void kahan_add(double& s, double& c, double x) {
+  const double y = x - c;
+  const double u = s + y;
+  c = (u - s) - y;
+  s = u;
+}
+
+template <typename Tin>
+__global__ void __launch_bounds__(256) solve_partials_kernel(const Tin* __restrict__ x, long long n, double* part) {
+  const long long b = blockIdx.y;
+  const long long chunk = (n + kSumBlocks - 1) / kSumBlocks;
+  const long long lo = blockIdx.x * chunk, hi = lo + chunk < n ? lo + chunk : n;
+  const Tin* xs = x + b * n;
+  double s = 0, c = 0;
+  for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    if (sizeof(Tin) == sizeof(double)) kahan_add(s, c, (double)xs[i]);
+    else s += (double)xs[i];
+  }
+  for (int off = 16; off > 0; off /= 2) s += __shfl_xor_sync(0xffffffffu, s, off);
+  __shared__ double ws[8];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x / 32] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0, tc = 0;
+    for (int k = 0; k < (int)(blockDim.x / 32); ++k) kahan_add(t, tc, ws[k]);
+    part[b * kSumBlocks + blockIdx.x] = t;
+  }
+}
+
+__global__ void solve_sums_finish_kernel(const double* __restrict__ part, double* out, int out_stride) {
+  const int b = blockIdx.x;
+  double s = 0, c = 0;
+  for (int k = threadIdx.x; k < kSumBlocks; k += 32) kahan_add(s, c, part[b * kSumBlocks + k]);
+  for (int off = 16; off > 0; off /= 2) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if (threadIdx.x == 0) out[(long long)b * out_stride] = s;
+}
+
+template <typename Tin>
+cudaError_t launch_solve_sums(const Tin* x, long long n, int batch, double* partials, double* out, int out_stride,
+                              cudaStream_t st) {
+  solve_partials_kernel<Tin><<<dim3(kSumBlocks, batch), 256, 0, st>>>(x, n, partials);
+  solve_sums_finish_kernel<<<batch, 32, 0, st>>>(partials, out, out_stride);
+  return cudaGetLastError();
+}
+
+// k0[4b] = Re src[b * per_solve] (the (0,0) element of a solve's spectrum)
+__global__ void k0_from_spec_kernel(const double2* __restrict__ src, long long per_solve, int batch, double* k0) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < batch) k0[4 * b] = src[(long long)b * per_solve].x;
+}
+// dst[b * per_solve] = (k0[4b], 0)
+__global__ void k0_to_spec_kernel(double2* dst, long long per_solve, int batch, const double* __restrict__ k0) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < batch) dst[(long long)b * per_solve] = make_double2(k0[4 * b], 0.0);
+}
+cudaError_t launch_k0_from_spec(const double2* src, long long per_solve, int batch, double* k0, cudaStream_t st) {
+  k0_from_spec_kernel<<<(batch + 127) / 128, 128, 0, st>>>(src, per_solve, batch, k0);
+  return cudaGetLastError();
+}
+cudaError_t launch_k0_to_spec(double2* dst, long long per_solve, int batch, const double* k0, cudaStream_t st) {
+  k0_to_spec_kernel<<<(batch + 127) / 128, 128, 0, st>>>(dst, per_solve, batch, k0);
+  return cudaGetLastError();
+}
+
+// dst = src + (k0[4b] - sums[b]) / n for solve b: the field's sum becomes the
+// FP64 (0,0) mode.
+template <typename T>
+__global__ void real_out_shift_kernel(const T* __restrict__ src, double* __restrict__ dst, long long n, int batch,
+                                      const double* __restrict__ k0, const double* __restrict__ sums) {
+  const long long tot = n * batch;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    const long long b = i / n;
+    dst[i] = (double)src[i] + (k0[4 * b] - sums[b]) / (double)n;
+  }
+}
+template <typename T>
+cudaError_t launch_real_out_shift(const T* src, double* dst, long long n, int batch, const double* k0,
+                                  const double* sums, cudaStream_t st) {
+  real_out_shift_kernel<T><<<grid_for(n * batch), 256, 0, st>>>(src, dst, n, batch, k0, sums);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_solve_sums<double>(const double*, long long, int, double*, double*, int, cudaStream_t);
+template cudaError_t launch_solve_sums<float>(const float*, long long, int, double*, double*, int, cudaStream_t);
+template cudaError_t launch_real_out_shift<float>(const float*, double*, long long, int, const double*, const double*,
+                                                  cudaStream_t);
+template cudaError_t launch_real_out_shift<double>(const double*, double*, long long, int, const double*, const double*,
+                                                   cudaStream_t);
+
 template cudaError_t launch_real_in<double>(const double*, double*, long long, double, cudaStream_t);
 template cudaError_t launch_real_in<float>(const double*, float*, long long, double, cudaStream_t);
 template cudaError_t launch_real_out<double>(const double*, double*, long long, cudaStream_t);

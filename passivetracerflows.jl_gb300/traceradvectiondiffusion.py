@@ -195,7 +195,9 @@ class Problem:
     Extensions (keyword-only): ``κh``/``nκh`` (hyperdiffusion, reachable in the
     reference only through ``ConstDiffSteadyFlowParams``), ``batch`` (independent
     solves sharing grid, parameters and flow), ``time_mode`` ("clock" as the
-    reference, or "stage").  ``T=np.float32`` selects the FP32 form.
+    reference, or "stage").  ``T=np.float32`` selects the FP32 form, in which
+    ``k0_fp64`` (default True) carries the conserved (0,0[,0]) mode -- state,
+    stage combinations and the mean reported by ``vars.c`` -- in FP64.
     """
 
     def __init__(self, dev, advecting_flow: AdvectingFlow, **kwargs):
@@ -221,6 +223,7 @@ class Problem:
         T = kwargs.pop("T", np.float64)
         batch = int(kwargs.pop("batch", 1))
         time_mode = kwargs.pop("time_mode", "clock")
+        k0_fp64 = bool(kwargs.pop("k0_fp64", True))
         if kwargs:
             raise TypeError(f"unexpected keyword arguments: {sorted(kwargs)}")
         steppers = {"RK4": L.PTF_RK4, "ETDRK4": L.PTF_ETDRK4}
@@ -244,6 +247,7 @@ class Problem:
         cfg.precision = prec
         cfg.time_mode = {"clock": L.PTF_CLOCK_T, "stage": L.PTF_STAGE_T}[time_mode]
         cfg.batch = batch
+        cfg.k0_mode = 1 if k0_fp64 else 0
         h = ct.c_void_p()
         L.check(lib.ptf_create(ct.byref(cfg), ct.byref(h)), None)
         self._h = h
@@ -325,6 +329,40 @@ class Problem:
         L.check(L.load().ptf_calcN(self._h, a.ctypes.data_as(ct.c_void_p), out.ctypes.data_as(ct.c_void_p),
                                    L.PTF_HOST), self._h)
         return out
+
+    def set_schedule(self, solves_per_group=0, branches=1, use_graph=True):
+        """Step a batch in groups of solves (0: whole batch, or batch/branches),
+        dealt to `branches` concurrent stream branches, replaying steps from a
+        captured CUDA graph; results do not depend on the schedule."""
+        L.check(L.load().ptf_set_schedule(self._h, int(solves_per_group), int(branches), 1 if use_graph else 0),
+                self._h)
+
+    _TUNING_FIELDS = ("col_lines", "col_lines_y", "row_pairs", "branches", "solves_per_group", "row_staged",
+                      "ms_per_step")
+
+    @property
+    def tuning(self):
+        """Launch shapes of this problem (columns / row pairs per block,
+        branches, staged row pass) and the tuned ms per step (0: untuned)."""
+        t = L.PtfTuning()
+        L.check(L.load().ptf_get_tuning(self._h, ct.byref(t)), self._h)
+        return {k: getattr(t, k) for k in self._TUNING_FIELDS}
+
+    @tuning.setter
+    def tuning(self, value):
+        t = L.PtfTuning()
+        L.check(L.load().ptf_get_tuning(self._h, ct.byref(t)), self._h)
+        for k, v in dict(value).items():
+            if k not in self._TUNING_FIELDS:
+                raise KeyError(k)
+            setattr(t, k, v)
+        L.check(L.load().ptf_set_tuning(self._h, ct.byref(t)), self._h)
+
+    def autotune(self, trial_steps=4, force=False):
+        """Time candidate launch shapes on this problem (state saved and
+        restored) and keep the fastest; cached per shape for the process."""
+        L.check(L.load().ptf_autotune(self._h, int(trial_steps), L.PTF_TUNE_FORCE if force else 0), self._h)
+        return self.tuning
 
     def synchronize(self):
         L.check(L.load().ptf_synchronize(self._h), self._h)
