@@ -56,8 +56,8 @@ enum ptf_where { PTF_HOST = 0, PTF_DEVICE = 1 };
  * hyperdiffusion of ConstDiffSteadyFlowParams (:436-452), which the
  * reference reaches only through its low-level constructor. */
 typedef struct ptf_config {
-  int32_t dim;        /* 2 or 3 */
-  int32_t nx, ny, nz; /* powers of two, 16..4096 (nz ignored for dim 2) */
+  int32_t dim;        /* 1, 2 or 3 */
+  int32_t nx, ny, nz; /* powers of two, 16..4096 (ny, nz ignored below their dim) */
   double Lx, Ly, Lz;
   double kappa, eta, iota; /* x, y, z diffusivities */
   double kappah;           /* hyperdiffusivity */
@@ -79,13 +79,15 @@ typedef struct ptf_handle ptf_handle;
 void ptf_config_default(ptf_config* cfg, int32_t dim);
 
 /* TracerAdvectionDiffusion.Problem(dev, flow; ...) construction:
- * grid (:177,:205), Equation L (:538-554), Vars (:652-668) and the
- * FourierFlows time stepper state (FourierFlows.Problem, :187,:215). */
+ * 1D (:143-163), 2D (:165-188), 3D (:190-216); grid (:158,:177,:205),
+ * Equation L (:538-554), Vars (:652-668) and the FourierFlows time stepper
+ * state (FourierFlows.Problem, :162,:187,:215).  1D problems step a batch
+ * of solves in pairs (an odd batch carries one zero solve on the device). */
 int ptf_create(const ptf_config* cfg, ptf_handle** out);
 void ptf_destroy(ptf_handle* h);
 const char* ptf_last_error(const ptf_handle* h);
 
-/* Steady flow arrays u.(x,y[,z]), v, w on the grid: the precomputation of
+/* Steady flow arrays u.(x[,y,z]), v, w on the grid (v from 2D, w in 3D): the precomputation of
  * ConstDiffSteadyFlowParams (:436-452).  Also used for a time-varying flow
  * re-evaluated by the caller at clock.t before each step (:715-718). */
 int ptf_set_flow_arrays(ptf_handle* h, const double* u, const double* v, const double* w, int32_t where);
@@ -106,7 +108,7 @@ int ptf_step(ptf_handle* h, int64_t nsteps);
 int ptf_clock(const ptf_handle* h, double* t, int64_t* step);
 int ptf_set_clock(ptf_handle* h, double t, int64_t step);
 
-/* calcN!(N, sol, t, clock, vars, params, grid) (:756-769 / :771-786): the
+/* calcN!(N, sol, t, clock, vars, params, grid) (:744-754 / :756-769 / :771-786): the
  * FourierFlows Equation plugin on its own: N = rfft(-(u.grad c)) for the
  * spectral field `sol`, with the flow set on the handle.  Complex arrays. */
 int ptf_calcN(ptf_handle* h, const double* sol, double* N, int32_t where);
@@ -130,11 +132,14 @@ int ptf_set_schedule(ptf_handle* h, int32_t solves_per_group, int32_t branches, 
  * per row-pass block; branches / solves_per_group: as ptf_set_schedule;
  * row_staged: 2D RHS row pass staging its rows in shared memory with bulk
  * copies (falls back to the direct kernel where that does not fit);
+ * col_carveout: the share of the SM's L1/shared storage the column passes
+ * ask to be shared memory (the rest caches, among others, register spills);
  * ms_per_step: the time measured by ptf_autotune (0 when not tuned).  Line
  * counts are powers of two dividing the lines of the pass, within the
  * block's resource limit.  Shapes do not change results. */
 typedef struct ptf_tuning {
   int32_t col_lines, col_lines_y, row_pairs, branches, solves_per_group, row_staged;
+  int32_t col_carveout; /* column passes' preferred shared-memory carve-out, percent (-1: driver's choice) */
   double ms_per_step;
 } ptf_tuning;
 enum { PTF_TUNE_FORCE = 1 };

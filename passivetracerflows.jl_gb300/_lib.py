@@ -64,7 +64,7 @@ class PtfServerStats(ct.Structure):
 class PtfTuning(ct.Structure):
     _fields_ = [("col_lines", ct.c_int32), ("col_lines_y", ct.c_int32), ("row_pairs", ct.c_int32),
                 ("branches", ct.c_int32), ("solves_per_group", ct.c_int32), ("row_staged", ct.c_int32),
-                ("ms_per_step", ct.c_double)]
+                ("col_carveout", ct.c_int32), ("ms_per_step", ct.c_double)]
 
 
 PTF_TUNE_FORCE = 1

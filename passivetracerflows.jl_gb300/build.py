@@ -36,6 +36,7 @@ INST_SOURCES = {
     "ptf_k2d_inst.cu": [(f"{t}_{n}", [f"-DPTF_T={t}", f"-DPTF_N={n}"]) for t in ("float", "double") for n in _SIZES],
     "ptf_batch_inst.cu": [(f"{t}_m{m}", [f"-DPTF_T={t}", f"-DPTF_MODE={m}"]) for t in ("float", "double")
                           for m in (2, 3, 4, 5)],
+    "ptf_k1d_inst.cu": [(f"{t}_{n}", [f"-DPTF_T={t}", f"-DPTF_N={n}"]) for t in ("float", "double") for n in _SIZES],
 }
 
 

@@ -98,6 +98,7 @@ template <typename F> void parallel_for(long long n, F f) {
 // stride `stride`, ncols flat columns, nblk_y blocks of fields bstride apart.
 struct ColGeom {
   int n = 0, stride = 0, ncols = 0, nblk_y = 0, W = 1;
+  int carve = -1;  // preferred shared-memory carve-out in percent (-1: the driver's choice)
   long long bstride = 0;
   double dk = 0;
   int axis = 0;  // 1 = y, 2 = z
@@ -114,6 +115,7 @@ struct ptf_handle {
   long long plane = 0;      // spectral elements per solve (nz*ny*pitch)
   long long nphys = 0;      // physical points per solve (nz*ny*nx)
   long long rows = 0;       // x rows per solve (nz*ny)
+  int bpad = 1;             // solves held on the device: 1D rounds the batch up to pairs
   bool fp32 = false;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
@@ -202,13 +204,13 @@ template <typename T> int upload(ptf_handle* h, void* dst, const std::vector<T>&
 template <typename T> int upload_tables(ptf_handle* h) {
   const ptf_config& c = h->cfg;
   const int ny = h->ny, nz = h->nz, pitch = h->pitch, nkr = h->nkr;
-  const double dkx = 2 * M_PI / c.Lx, dky = 2 * M_PI / c.Ly, dkz = h->dim == 3 ? 2 * M_PI / c.Lz : 0.0;
+  const double dkx = 2 * M_PI / c.Lx, dky = h->dim >= 2 ? 2 * M_PI / c.Ly : 0.0, dkz = h->dim == 3 ? 2 * M_PI / c.Lz : 0.0;
   const size_t plane = (size_t)h->plane;
   std::vector<double> L(plane, 0.0);
   for (int q = 0; q < nz; ++q) {
     const double m = h->dim == 3 ? (q < nz / 2 ? q : q - nz) * dkz : 0.0;
     for (int j = 0; j < ny; ++j) {
-      const double l = (j < ny / 2 ? j : j - ny) * dky;
+      const double l = h->dim == 1 ? 0.0 : (j < ny / 2 ? j : j - ny) * dky;
       for (int k = 0; k < nkr; ++k) {
         const double kr = k * dkx;
         const double krsq = kr * kr + l * l + m * m;
@@ -260,8 +262,10 @@ template <typename T> int upload_tables(ptf_handle* h) {
   std::vector<T> tw;
   fill_twiddles(tw, h->nx);
   if ((rc = upload(h, h->twx, tw, "upload twiddles"))) return rc;
-  fill_twiddles(tw, h->ny);
-  if ((rc = upload(h, h->twy, tw, "upload twiddles"))) return rc;
+  if (h->dim >= 2) {
+    fill_twiddles(tw, h->ny);
+    if ((rc = upload(h, h->twy, tw, "upload twiddles"))) return rc;
+  }
   if (h->dim == 3) {
     fill_twiddles(tw, h->nz);
     if ((rc = upload(h, h->twz, tw, "upload twiddles"))) return rc;
@@ -281,6 +285,18 @@ double pass_bytes(const ptf_handle* h, int kind, int mode) {
   const double M = ne * e, Tb = ne * r;
   const double P = (double)h->nphys * r;
   const double B = (double)h->cfg.batch;
+  if (kind == 2) {  // 1D stage pass: stage input + state traffic, flow
+    switch (mode) {
+      case COL_FWD_N: return B * 2 * M + P;
+      case COL_RK4_1: return B * 3 * M + Tb + P;
+      case COL_RK4_2: case COL_RK4_3: return B * 5 * M + Tb + P;
+      case COL_RK4_4: return B * 3 * M + Tb + P;
+      case COL_ETD_1: return B * 4 * M + 4 * Tb + P;
+      case COL_ETD_2: return B * 5 * M + 3 * Tb + P;
+      case COL_ETD_3: return B * 6 * M + 3 * Tb + P;
+      default: return B * 3 * M + Tb + P;  // COL_ETD_4
+    }
+  }
   if (kind == 1) {  // row pass
     if (mode == ROW_RHS) return B * 3 * M + 2 * P;
     if (mode == ROW_RHS3) return B * 4 * M + 3 * P;
@@ -371,7 +387,7 @@ template <typename T> int run_col(ptf_handle* h, const ColGeom& g, int mode, con
   cudaStream_t st = gr.st ? gr.st : h->stream;
   cudaEvent_t e0;
   prof_begin(h, &e0, st);
-  cudaError_t e = launch_col<T>(g.n, a, g.W, g.ncols / g.W, nblk_y, st);
+  cudaError_t e = launch_col<T>(g.n, a, g.W, g.ncols / g.W, nblk_y, st, g.carve);
   prof_end(h, e0, 0, pass_bytes(h, 0, mode) * gr.nb / h->cfg.batch, st);
   h->launches++;
   if (e != cudaSuccess) return cuda_fail(h, e, "column pass launch");
@@ -399,14 +415,42 @@ int run_row(ptf_handle* h, int mode, const void* A, const void* B, const void* C
   a.tma = (h->row_tma && h->dim == 2 && mode == ROW_RHS) ? 1 : 0;
   a.bstride = h->plane; a.pstride = h->nphys; a.fstride = 0;
   const int P = h->rowP;
-  const int nby = (int)((h->rows / 2) / P);
+  int nby = (int)((h->rows / 2) / P), nfields = gr.nb;
+  if (h->dim == 1) {  // one row per solve: the pairs run over the (padded) batch
+    a.rows = h->bpad;
+    a.bstride = 0; a.pstride = 0;
+    nby = (h->bpad / 2) / P;
+    nfields = 1;
+  }
   cudaStream_t st = gr.st ? gr.st : h->stream;
   cudaEvent_t e0;
   prof_begin(h, &e0, st);
-  cudaError_t e = launch_row<T>(h->nx, a, P, nby, gr.nb, st);
+  cudaError_t e = launch_row<T>(h->nx, a, P, nby, nfields, st);
   prof_end(h, e0, 1, pass_bytes(h, 1, mode) * gr.nb / h->cfg.batch, st);
   h->launches++;
   if (e != cudaSuccess) return cuda_fail(h, e, "row pass launch");
+  return PTF_OK;
+}
+
+// One 1D stage pass over every solve: stage input xin, next input xout.
+template <typename T> int run_line1d(ptf_handle* h, int mode, const void* xin, void* xout) {
+  typedef typename cplx_of<T>::type C;
+  Line1DArgs<T> a;
+  std::memset(&a, 0, sizeof(a));
+  a.xin = (const C*)xin; a.xout = (C*)xout;
+  a.s = (C*)h->s; a.si = (C*)h->si; a.acc = (C*)h->acc; a.n1 = (C*)h->n1;
+  a.u = (const T*)h->u; a.Ltab = (const T*)h->Ltab; a.coef = (const T*)h->coef; a.tw = (const C*)h->twx;
+  a.dkx = (T)(2 * M_PI / h->cfg.Lx);
+  a.dt = (T)h->cfg.dt;
+  a.pitch = h->pitch; a.rows = h->bpad;
+  if (h->k0mode && mode != COL_FWD_N) { a.k0 = h->k0; a.k0c = h->k0c; a.dt64 = h->cfg.dt; }
+  const int P = h->rowP;
+  cudaEvent_t e0;
+  prof_begin(h, &e0, h->stream);
+  cudaError_t e = launch_line1d<T>(h->nx, mode, a, P, (h->bpad / 2) / P, h->stream);
+  prof_end(h, e0, 1, pass_bytes(h, 2, mode), h->stream);
+  h->launches++;
+  if (e != cudaSuccess) return cuda_fail(h, e, "1D stage pass launch");
   return PTF_OK;
 }
 
@@ -482,6 +526,21 @@ int auto_group(const ptf_handle* h) {
 // same time; within a branch the groups follow one another.
 template <typename T> int enqueue_step(ptf_handle* h, int group) {
   const bool etd = h->cfg.stepper == PTF_ETDRK4;
+  if (h->dim == 1) {
+    // stage inputs: RK4 s, si, si, si (si updated in place); ETDRK4 s, a (si),
+    // b (A), c (A, in place)
+    int rc;
+    if (etd) {
+      if ((rc = run_line1d<T>(h, COL_ETD_1, h->s, nullptr))) return rc;
+      if ((rc = run_line1d<T>(h, COL_ETD_2, h->si, h->A))) return rc;
+      if ((rc = run_line1d<T>(h, COL_ETD_3, h->A, h->A))) return rc;
+      return run_line1d<T>(h, COL_ETD_4, h->A, nullptr);
+    }
+    if ((rc = run_line1d<T>(h, COL_RK4_1, h->s, nullptr))) return rc;
+    if ((rc = run_line1d<T>(h, COL_RK4_2, h->si, nullptr))) return rc;
+    if ((rc = run_line1d<T>(h, COL_RK4_3, h->si, nullptr))) return rc;
+    return run_line1d<T>(h, COL_RK4_4, h->si, nullptr);
+  }
   const int nbr = std::max(1, std::min(h->branches, 4));
   if (nbr > 1) {
     for (int k = 0; k < nbr - 1; ++k) {
@@ -529,7 +588,7 @@ void drop_graph(ptf_handle* h) {
 }
 
 template <typename T> int do_steps(ptf_handle* h, long long nsteps) {
-  if (!h->ab_valid) { int rc = do_prologue<T>(h); if (rc) return rc; }
+  if (!h->ab_valid && h->dim >= 2) { int rc = do_prologue<T>(h); if (rc) return rc; }
   int group = h->group > 0 ? std::min(h->group, (int)h->cfg.batch) : auto_group(h);
   if (h->branches > 1 && h->group == 0) group = (h->cfg.batch + h->branches - 1) / h->branches;
   // Replay a captured step unless per-pass timing is on (it records events
@@ -554,7 +613,7 @@ template <typename T> int do_steps(ptf_handle* h, long long nsteps) {
       h->graph_group = group;
     }
   }
-  const int per_step = (int)(((h->cfg.batch + group - 1) / group) * 4 * (h->dim == 3 ? 4 : 2));
+  const int per_step = h->dim == 1 ? 4 : (int)(((h->cfg.batch + group - 1) / group) * 4 * (h->dim == 3 ? 4 : 2));
   for (long long n = 0; n < nsteps; ++n) {
     if (graph) {
       cudaError_t e = cudaGraphLaunch(h->gexec, h->stream);
@@ -590,8 +649,8 @@ template <typename T> int phys_in(ptf_handle* h, const double* src, int where, T
 }
 
 // FP64 k = 0 mode scratch: sum partials and per-solve sums
-double* k0_partials(const ptf_handle* h) { return h->k0 + 4 * (size_t)h->cfg.batch; }
-double* k0_sums(const ptf_handle* h) { return h->k0 + 68 * (size_t)h->cfg.batch; }
+double* k0_partials(const ptf_handle* h) { return h->k0 + 4 * (size_t)h->bpad; }
+double* k0_sums(const ptf_handle* h) { return h->k0 + 68 * (size_t)h->bpad; }
 
 template <typename T> int set_c_impl(ptf_handle* h, const double* c, int where) {
   int rc = phys_in<T>(h, c, where, (T*)h->phys, h->nphys * h->cfg.batch, 1.0);
@@ -602,6 +661,12 @@ template <typename T> int set_c_impl(ptf_handle* h, const double* c, int where) 
     cudaError_t e = launch_solve_sums<double>(dsrc, h->nphys, h->cfg.batch, k0_partials(h), h->k0, 4, h->stream);
     h->launches += 2;
     if (e != cudaSuccess) return cuda_fail(h, e, "k = 0 mode sum");
+  }
+  if (h->dim == 1) {  // sol = rfft(c) of every solve, straight into the state
+    rc = run_row<T>(h, ROW_R2C, nullptr, nullptr, nullptr, h->s, h->phys, nullptr, 0.5);
+    if (rc) return rc;
+    h->ab_valid = true;
+    return PTF_OK;
   }
   void* nx = h->dim == 2 ? h->Nx : h->A;
   rc = run_row<T>(h, ROW_R2C, nullptr, nullptr, nullptr, nx, h->phys, nullptr, 0.5);
@@ -625,10 +690,10 @@ template <typename T> int set_c_impl(ptf_handle* h, const double* c, int where) 
 
 template <typename T> int get_c_impl(ptf_handle* h, double* dst) {
   int rc = PTF_OK;
-  if (!h->ab_valid) rc = do_prologue<T>(h);
+  if (!h->ab_valid && h->dim >= 2) rc = do_prologue<T>(h);
   if (rc) return rc;
   const double inv = 1.0 / (double)h->nphys;
-  rc = run_row<T>(h, ROW_C2R, h->A, nullptr, nullptr, nullptr, nullptr, h->phys, inv);
+  rc = run_row<T>(h, ROW_C2R, h->dim == 1 ? h->s : h->A, nullptr, nullptr, nullptr, nullptr, h->phys, inv);
   if (rc) return rc;
   const long long n = h->nphys * h->cfg.batch;
   cudaError_t e;
@@ -647,6 +712,7 @@ template <typename T> int get_c_impl(ptf_handle* h, double* dst) {
 }
 
 template <typename T> int calcN_impl(ptf_handle* h, void* sbuf) {
+  if (h->dim == 1) return run_line1d<T>(h, COL_FWD_N, sbuf, sbuf);  // N replaces the input in place
   int rc = do_prologue<T>(h, sbuf);
   if (!rc) rc = rhs_and_column<T>(h, COL_FWD_N, sbuf, false);
   h->ab_valid = false;
@@ -723,6 +789,7 @@ ptf_tuning current_tuning(const ptf_handle* h) {
   t.branches = h->branches;
   t.solves_per_group = h->group;
   t.row_staged = h->row_tma;
+  t.col_carveout = h->gmain.carve;
   t.ms_per_step = h->tuned_ms;
   return t;
 }
@@ -733,17 +800,21 @@ bool lines_ok(const ptf_handle* h, int n, bool col, int W, long long divisor) {
   return W <= mx;
 }
 
+long long row_pairs_total(const ptf_handle* h) { return h->dim == 1 ? h->bpad / 2 : h->rows / 2; }
+
 int apply_tuning(ptf_handle* h, const ptf_tuning& t) {
-  if (!lines_ok(h, h->gmain.n, true, t.col_lines, h->gmain.ncols))
+  if (h->dim >= 2 && !lines_ok(h, h->gmain.n, true, t.col_lines, h->gmain.ncols))
     return fail(h, PTF_ERR_ARG, "col_lines: a power of two dividing the columns, within the block limit");
   if (h->dim == 3 && !lines_ok(h, h->gy3.n, true, t.col_lines_y, h->gy3.ncols))
     return fail(h, PTF_ERR_ARG, "col_lines_y: a power of two dividing the columns, within the block limit");
-  if (!lines_ok(h, h->nx, false, t.row_pairs, h->rows / 2))
+  if (!lines_ok(h, h->nx, false, t.row_pairs, row_pairs_total(h)))
     return fail(h, PTF_ERR_ARG, "row_pairs: a power of two dividing the row pairs, within the block limit");
-  if (t.branches < 1 || t.branches > 4) return fail(h, PTF_ERR_ARG, "branches must be 1..4");
+  if (t.branches < 1 || t.branches > 4 || (h->dim == 1 && t.branches != 1))
+    return fail(h, PTF_ERR_ARG, "branches must be 1..4 (1 for 1D problems)");
   if (t.solves_per_group < 0) return fail(h, PTF_ERR_ARG, "solves_per_group must be >= 0");
   if (t.row_staged != 0 && t.row_staged != 1) return fail(h, PTF_ERR_ARG, "row_staged must be 0 or 1");
-  h->gmain.W = t.col_lines;
+  if (t.col_carveout < -1 || t.col_carveout > 100) return fail(h, PTF_ERR_ARG, "col_carveout must be -1..100");
+  if (h->dim >= 2) { h->gmain.W = t.col_lines; h->gmain.carve = t.col_carveout; h->gy3.carve = t.col_carveout; }
   if (h->dim == 3) h->gy3.W = t.col_lines_y;
   h->rowP = t.row_pairs;
   h->branches = t.branches;
@@ -778,11 +849,11 @@ template <typename T> int time_steps(ptf_handle* h, int steps, double* ms) {
 
 template <typename T> int autotune_impl(ptf_handle* h, int steps) {
   typedef typename cplx_of<T>::type C;
-  const size_t sbytes = (size_t)h->plane * h->cfg.batch * sizeof(C);
+  const size_t sbytes = (size_t)h->plane * h->bpad * sizeof(C);
   void* saved = nullptr;
   double* saved_k0 = nullptr;
   if (cudaMalloc(&saved, sbytes) != cudaSuccess) { cudaGetLastError(); return fail(h, PTF_ERR_MEMORY, "tuning: state copy"); }
-  if (h->k0mode && cudaMalloc((void**)&saved_k0, 4 * sizeof(double) * h->cfg.batch) != cudaSuccess) {
+  if (h->k0mode && cudaMalloc((void**)&saved_k0, 4 * sizeof(double) * h->bpad) != cudaSuccess) {
     cudaGetLastError();
     cudaFree(saved);
     return fail(h, PTF_ERR_MEMORY, "tuning: state copy");
@@ -791,7 +862,7 @@ template <typename T> int autotune_impl(ptf_handle* h, int steps) {
   const long long step0 = h->step;
   cudaError_t e = cudaMemcpyAsync(saved, h->s, sbytes, cudaMemcpyDeviceToDevice, h->stream);
   if (e == cudaSuccess && saved_k0)
-    e = cudaMemcpyAsync(saved_k0, h->k0, 4 * sizeof(double) * h->cfg.batch, cudaMemcpyDeviceToDevice, h->stream);
+    e = cudaMemcpyAsync(saved_k0, h->k0, 4 * sizeof(double) * h->bpad, cudaMemcpyDeviceToDevice, h->stream);
   int rc = e == cudaSuccess ? PTF_OK : cuda_fail(h, e, "tuning: save state");
 
   ptf_tuning best = current_tuning(h);
@@ -806,14 +877,18 @@ template <typename T> int autotune_impl(ptf_handle* h, int steps) {
   };
   if (!rc) rc = trial(best);
   // one knob at a time, starting from the best so far
-  for (int knob = 0; knob < 5 && !rc; ++knob) {
+  for (int knob = 0; knob < 6 && !rc; ++knob) {
     std::vector<ptf_tuning> cands;
-    for (int v = 1; v <= 64; v *= 2) {
+    if (knob == 5) {  // shared-memory carve-out of the column passes (L1 left for register spills)
+      if (h->dim >= 2)
+        for (int pct : {-1, 50, 60, 70, 80, 90, 100}) { ptf_tuning t = best; t.col_carveout = pct; cands.push_back(t); }
+    }
+    for (int v = 1; v <= 64 && knob < 5; v *= 2) {
       ptf_tuning t = best;
-      if (knob == 0) { if (!lines_ok(h, h->gmain.n, true, v, h->gmain.ncols)) continue; t.col_lines = v; }
+      if (knob == 0) { if (h->dim < 2 || !lines_ok(h, h->gmain.n, true, v, h->gmain.ncols)) continue; t.col_lines = v; }
       else if (knob == 1) { if (h->dim != 3 || !lines_ok(h, h->gy3.n, true, v, h->gy3.ncols)) continue; t.col_lines_y = v; }
-      else if (knob == 2) { if (!lines_ok(h, h->nx, false, v, h->rows / 2)) continue; t.row_pairs = v; }
-      else if (knob == 3) { if (v > 4 || v > h->cfg.batch) continue; t.branches = v; t.solves_per_group = 0; }
+      else if (knob == 2) { if (!lines_ok(h, h->nx, false, v, row_pairs_total(h))) continue; t.row_pairs = v; }
+      else if (knob == 3) { if (v > 4 || v > h->cfg.batch || h->dim == 1) continue; t.branches = v; t.solves_per_group = 0; }
       else { if (v > 2 || h->dim != 2) continue; t.row_staged = v - 1; }
       cands.push_back(t);
     }
@@ -826,7 +901,7 @@ template <typename T> int autotune_impl(ptf_handle* h, int steps) {
   // restore the solve
   e = cudaMemcpyAsync(h->s, saved, sbytes, cudaMemcpyDeviceToDevice, h->stream);
   if (e == cudaSuccess && saved_k0)
-    e = cudaMemcpyAsync(h->k0, saved_k0, 4 * sizeof(double) * h->cfg.batch, cudaMemcpyDeviceToDevice, h->stream);
+    e = cudaMemcpyAsync(h->k0, saved_k0, 4 * sizeof(double) * h->bpad, cudaMemcpyDeviceToDevice, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   cudaFree(saved);
   if (saved_k0) cudaFree(saved_k0);
@@ -885,12 +960,11 @@ int ptf_create(const ptf_config* cfg, ptf_handle** out) {
   if (!cfg || !out) return fail(nullptr, PTF_ERR_ARG, "ptf_create: null argument");
   *out = nullptr;
   const ptf_config c = *cfg;
-  if (c.dim == 1) return fail(nullptr, PTF_ERR_UNSUPPORTED, "1D problems are not built in this library");
-  if (c.dim != 2 && c.dim != 3) return fail(nullptr, PTF_ERR_ARG, "dim must be 2 or 3");
+  if (c.dim < 1 || c.dim > 3) return fail(nullptr, PTF_ERR_ARG, "dim must be 1, 2 or 3");
   auto okn = [](int n) { return is_pow2(n) && n >= 16 && n <= 4096; };
-  if (!okn(c.nx) || !okn(c.ny) || (c.dim == 3 && !okn(c.nz)))
-    return fail(nullptr, PTF_ERR_ARG, "nx, ny (and nz) must be powers of two in [16, 4096]");
-  if (!(c.Lx > 0) || !(c.Ly > 0) || (c.dim == 3 && !(c.Lz > 0)))
+  if (!okn(c.nx) || (c.dim >= 2 && !okn(c.ny)) || (c.dim == 3 && !okn(c.nz)))
+    return fail(nullptr, PTF_ERR_ARG, "nx (ny, nz) must be powers of two in [16, 4096]");
+  if (!(c.Lx > 0) || (c.dim >= 2 && !(c.Ly > 0)) || (c.dim == 3 && !(c.Lz > 0)))
     return fail(nullptr, PTF_ERR_ARG, "domain lengths must be positive");
   if (!(c.dt > 0) || !std::isfinite(c.dt)) return fail(nullptr, PTF_ERR_ARG, "dt must be positive and finite");
   if (c.stepper != PTF_RK4 && c.stepper != PTF_ETDRK4) return fail(nullptr, PTF_ERR_ARG, "stepper must be RK4 or ETDRK4");
@@ -905,7 +979,8 @@ int ptf_create(const ptf_config* cfg, ptf_handle** out) {
   ptf_handle* h = new ptf_handle();
   h->cfg = c;
   h->dim = c.dim;
-  h->nx = c.nx; h->ny = c.ny; h->nz = c.dim == 3 ? c.nz : 1;
+  h->nx = c.nx; h->ny = c.dim >= 2 ? c.ny : 1; h->nz = c.dim == 3 ? c.nz : 1;
+  h->bpad = c.dim == 1 ? c.batch + (c.batch & 1) : c.batch;
   h->fp32 = c.precision == PTF_FP32;
   h->k0mode = h->fp32 && c.k0_mode == 1;
   h->nkr = c.nx / 2 + 1;
@@ -920,7 +995,9 @@ int ptf_create(const ptf_config* cfg, ptf_handle** out) {
   auto lines = [&](int n, bool col, int div) {
     return h->fp32 ? default_lines_per_block<float>(n, col, div) : default_lines_per_block<double>(n, col, div);
   };
-  if (h->dim == 2) {
+  if (h->dim == 1) {
+    // no column passes
+  } else if (h->dim == 2) {
     ColGeom& g = h->gmain;
     g.n = h->ny; g.stride = h->pitch; g.ncols = h->pitch; g.nblk_y = c.batch; g.bstride = h->plane;
     g.dk = 2 * M_PI / c.Ly; g.axis = 1; g.W = lines(h->ny, true, h->pitch);
@@ -932,23 +1009,26 @@ int ptf_create(const ptf_config* cfg, ptf_handle** out) {
     y.n = h->ny; y.stride = h->pitch; y.ncols = h->pitch; y.nblk_y = c.batch * h->nz;
     y.bstride = (long long)h->ny * h->pitch; y.dk = 2 * M_PI / c.Ly; y.axis = 1; y.W = lines(h->ny, true, h->pitch);
   }
-  h->rowP = lines(h->nx, false, (int)(h->rows / 2));
+  h->rowP = lines(h->nx, false, (int)(h->dim == 1 ? h->bpad / 2 : h->rows / 2));
   // two concurrent stream branches for batches (measured +4% on 16 x 1024^2)
-  h->branches = c.batch >= 2 ? 2 : 1;
-  const size_t B = (size_t)c.batch;
+  h->branches = (c.batch >= 2 && h->dim >= 2) ? 2 : 1;
+  const size_t B = (size_t)h->bpad;
   const size_t sc = (size_t)h->plane * B * elem_c(h);
   const size_t sp = (size_t)h->nphys * B * elem_r(h);
   bool ok = true;
   ok = ok && dev_alloc(h, &h->s, sc) && dev_alloc(h, &h->si, sc) && dev_alloc(h, &h->acc, sc);
   if (c.stepper == PTF_ETDRK4) ok = ok && dev_alloc(h, &h->n1, sc);
-  ok = ok && dev_alloc(h, &h->A, sc) && dev_alloc(h, &h->B, sc);
+  ok = ok && dev_alloc(h, &h->A, sc);
+  if (h->dim >= 2) ok = ok && dev_alloc(h, &h->B, sc);
   if (h->dim == 2) ok = ok && dev_alloc(h, &h->Nx, sc);
-  else { ok = ok && dev_alloc(h, &h->C, sc); h->Nx = h->A; }
+  else if (h->dim == 3) { ok = ok && dev_alloc(h, &h->C, sc); h->Nx = h->A; }
   ok = ok && dev_alloc(h, &h->Ltab, (size_t)h->plane * elem_r(h));
   if (c.stepper == PTF_ETDRK4) ok = ok && dev_alloc(h, &h->coef, 6 * (size_t)h->plane * elem_r(h));
-  ok = ok && dev_alloc(h, &h->twx, (size_t)h->nx * elem_c(h)) && dev_alloc(h, &h->twy, (size_t)h->ny * elem_c(h));
+  ok = ok && dev_alloc(h, &h->twx, (size_t)h->nx * elem_c(h));
+  if (h->dim >= 2) ok = ok && dev_alloc(h, &h->twy, (size_t)h->ny * elem_c(h));
   if (h->dim == 3) ok = ok && dev_alloc(h, &h->twz, (size_t)h->nz * elem_c(h));
-  ok = ok && dev_alloc(h, &h->u, (size_t)h->nphys * elem_r(h)) && dev_alloc(h, &h->v, (size_t)h->nphys * elem_r(h));
+  ok = ok && dev_alloc(h, &h->u, (size_t)h->nphys * elem_r(h));
+  if (h->dim >= 2) ok = ok && dev_alloc(h, &h->v, (size_t)h->nphys * elem_r(h));
   if (h->dim == 3) ok = ok && dev_alloc(h, &h->w, (size_t)h->nphys * elem_r(h));
   ok = ok && dev_alloc(h, &h->phys, sp);
   h->stage_elems = std::max<long long>(h->nphys * (long long)B, 2 * h->rows * h->nkr * (long long)B);
@@ -969,7 +1049,8 @@ int ptf_create(const ptf_config* cfg, ptf_handle** out) {
 
 int ptf_set_flow_arrays(ptf_handle* h, const double* u, const double* v, const double* w, int32_t where) {
   if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
-  if (!u || !v || (h->dim == 3 && !w)) return fail(h, PTF_ERR_ARG, "u, v (and w in 3D) are required");
+  if (!u || (h->dim >= 2 && !v) || (h->dim == 3 && !w))
+    return fail(h, PTF_ERR_ARG, "u (v in 2D/3D, w in 3D) are required");
   if (check_where(h, where)) return PTF_ERR_ARG;
   // The flow is shared by the batch: nphys values per component.
   const double sc = -1.0 / (2.0 * (double)h->nphys);

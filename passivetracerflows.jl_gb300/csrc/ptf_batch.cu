@@ -336,16 +336,16 @@ template <typename T> int build_plan(ptf_batch* b) {
     r.fscale = (T)(-1.0 / (2.0 * (double)k.n * k.n));
     const SlotParams<T>& s0 = host_slot<T>(b, k.slot_base + act[0]);
     r.dkx = s0.dkx;
-    int tpl = 1;
+    int tpl = 1, ctpl = 1;
     switch (k.n) {
-#define PTF_CASE(n) case n: tpl = pass_tpl<T, n>(); break;
+#define PTF_CASE(n) case n: tpl = pass_tpl<T, n>(); ctpl = col_tpl<T, n>(); break;
       PTF_BATCH_SIZES(PTF_CASE)
 #undef PTF_CASE
       default: return bfail(b, PTF_ERR_UNSUPPORTED, "grid size not built for the batched form");
     }
-    const int lines = kBatchThreads / tpl;
+    const int lines = kBatchThreads / tpl, clines = kBatchThreads / ctpl;
     bp.row_items = (int)(((long long)c.nslots * (k.n / 2) + lines - 1) / lines);
-    bp.col_items = (int)(((long long)c.nslots * k.pitch + lines - 1) / lines);
+    bp.col_items = (int)(((long long)c.nslots * k.pitch + clines - 1) / clines);
     ++nb;
   }
   std::vector<int> pbk;

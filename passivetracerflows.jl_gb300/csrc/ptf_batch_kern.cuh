@@ -28,9 +28,9 @@ template <typename T> struct BatchBounds { static constexpr int blocks = 1; };
 template <> struct BatchBounds<float> { static constexpr int blocks = 2; };
 
 template <typename T, int N> __host__ __device__ constexpr size_t batch_smem_n() {
-  // W = P = 256 / (N/E) lines per block for both passes
-  return col_smem_bytes<T, N>(kBatchThreads / pass_tpl<T, N>()) > row_smem_bytes<T, N>(kBatchThreads / pass_tpl<T, N>(), 1)
-             ? col_smem_bytes<T, N>(kBatchThreads / pass_tpl<T, N>())
+  // W = 256 / col_tpl columns, P = 256 / pass_tpl row pairs per block
+  return col_smem_bytes<T, N>(kBatchThreads / col_tpl<T, N>()) > row_smem_bytes<T, N>(kBatchThreads / pass_tpl<T, N>(), 1)
+             ? col_smem_bytes<T, N>(kBatchThreads / col_tpl<T, N>())
              : row_smem_bytes<T, N>(kBatchThreads / pass_tpl<T, N>(), 1);
 }
 template <typename T> size_t batch_smem_bytes() {

@@ -46,6 +46,16 @@ template <typename C, typename T> __device__ __forceinline__ C cmul_cs(C v, T c,
   C r; r.x = v.x * c - v.y * s; r.y = v.x * s + v.y * c; return r;
 }
 // v * w (forward twiddle) or v * conj(w) (inverse)
+template <typename C> __device__ __forceinline__ C cmul_plain(C a, C b) {
+  C r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+#ifndef PTF_TW_POW2
+#define PTF_TW_POW2 0
+#endif
+
 template <int DIR, typename C> __device__ __forceinline__ C cmul_tw(C v, C w) {
   C r;
   if (DIR < 0) { r.x = v.x * w.x - v.y * w.y; r.y = v.x * w.y + v.y * w.x; }
@@ -221,8 +231,22 @@ __device__ __forceinline__ void stage_compute(C* v, int t, const C* __restrict__
     const int j = t + q * (N / E);
     if (NS > 1) {
       const int k = j % NS;
+      if (PTF_TW_POW2 && R == 16 && sizeof(v[0].x) == 4) {
+        // FP32: load w^1, w^2, w^4, w^8 and form the other powers by at most
+        // three products (error a few ulp), a quarter of the table loads
+        const int b = k * (N / (NS * R));
+        C w[16];
+        w[1] = ldtw(tw, b); w[2] = ldtw(tw, 2 * b); w[4] = ldtw(tw, 4 * b); w[8] = ldtw(tw, 8 * b);
+        w[3] = cmul_plain(w[2], w[1]);
+        w[5] = cmul_plain(w[4], w[1]); w[6] = cmul_plain(w[4], w[2]); w[7] = cmul_plain(w[4], w[3]);
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[q * R + r] = cmul_tw<DIR>(v[q * R + r], ldtw(tw, r * k * (N / (NS * R))));
+        for (int r = 9; r < 16; ++r) w[r] = cmul_plain(w[8], w[r - 8]);
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[q * R + r] = cmul_tw<DIR>(v[q * R + r], w[r]);
+      } else {
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[q * R + r] = cmul_tw<DIR>(v[q * R + r], ldtw(tw, r * k * (N / (NS * R))));
+      }
     }
     DFT<R, DIR, C>::run(v + q * R);
   }
@@ -264,28 +288,41 @@ template <int N, int DIR, int E = FFT_E> __host__ __device__ constexpr int stage
 // pattern; on exit v[] holds the result in the last stage's pattern.
 // `line` is this line's shared-memory buffer.  Every thread of the block
 // must call this: it contains __syncthreads().
+template <int N, int DIR, int E, int S> struct StageNS {  // product of the radices of stages 0..S-1
+  static constexpr int value = stage_radix<N, DIR, E>(S - 1) * StageNS<N, DIR, E, S - 1>::value;
+};
+template <int N, int DIR, int E> struct StageNS<N, DIR, E, 0> { static constexpr int value = 1; };
+
+// Stages S..NST-1 of a transform: exchange through shared memory, then
+// compute stage S in registers.
+template <int N, int DIR, int E, int S, int NST> struct StagesFrom {
+  template <typename C> static __device__ __forceinline__ void run(C* v, int t, C* line, const C* __restrict__ tw) {
+    if constexpr (S < NST) {
+      constexpr int RP = stage_radix<N, DIR, E>(S - 1);
+      constexpr int R = stage_radix<N, DIR, E>(S);
+      constexpr int NSP = StageNS<N, DIR, E, S - 1>::value;
+      constexpr int NS = StageNS<N, DIR, E, S>::value;
+      __syncthreads();
+      stage_store<N, RP, NSP, E>(v, t, line);
+      __syncthreads();
+      stage_load<N, R, E>(v, t, line);
+      stage_compute<N, R, NS, DIR, E>(v, t, tw);
+      StagesFrom<N, DIR, E, S + 1, NST>::run(v, t, line, tw);
+    }
+  }
+};
+
+// Full transform of one line.  On entry v[] holds the first stage's read
+// pattern; on exit v[] holds the result in the last stage's pattern.
+// `line` is this line's shared-memory buffer.  Every thread of the block
+// must call this: it contains __syncthreads().
 template <int N, int DIR, int E = FFT_E, typename C>
 __device__ __forceinline__ void fft_line(C* v, int t, C* line, const C* __restrict__ tw) {
   constexpr int NST = Sched<N, E>::NSTAGES;
-  static_assert(NST >= 1 && NST <= 3, "FFT length must be 16..4096");
+  static_assert(NST >= 1 && NST <= 6, "unsupported FFT length / values per thread");
   constexpr int R0 = stage_radix<N, DIR, E>(0);
-  constexpr int R1 = stage_radix<N, DIR, E>(NST > 1 ? 1 : 0);
-  constexpr int R2 = stage_radix<N, DIR, E>(NST > 2 ? 2 : 0);
   stage_compute<N, R0, 1, DIR, E>(v, t, tw);
-  if (NST > 1) {
-    __syncthreads();
-    stage_store<N, R0, 1, E>(v, t, line);
-    __syncthreads();
-    stage_load<N, R1, E>(v, t, line);
-    stage_compute<N, R1, R0, DIR, E>(v, t, tw);
-  }
-  if (NST > 2) {
-    __syncthreads();
-    stage_store<N, R1, R0, E>(v, t, line);
-    __syncthreads();
-    stage_load<N, R2, E>(v, t, line);
-    stage_compute<N, R2, R0 * R1, DIR, E>(v, t, tw);
-  }
+  StagesFrom<N, DIR, E, 1, NST>::run(v, t, line, tw);
 }
 
 template <int N, int DIR, int E = FFT_E> struct FirstRadix {

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "ptf_passes.cuh"
+#include "ptf_pass1d.cuh"
 
 #include <string>
 
@@ -12,13 +13,21 @@ void set_global_error(const std::string& msg);
 
 // Pass launchers (ptf_kern2d.cu dispatching to ptf_k2d_inst.cu objects).
 // Column pass over transform length n: grid (nbx, nby), W columns per block.
-template <typename T> cudaError_t launch_col(int n, const ColArgs<T>& a, int W, int nbx, int nby, cudaStream_t st);
+// carve: preferred shared-memory carve-out in percent (-1: the driver's choice).
+template <typename T>
+cudaError_t launch_col(int n, const ColArgs<T>& a, int W, int nbx, int nby, cudaStream_t st, int carve = -1);
 // Row pass over x length nx: grid (nbx, batch), P row pairs per block.
 template <typename T> cudaError_t launch_row(int nx, const RowArgs<T>& a, int P, int nbx, int batch, cudaStream_t st);
 // Largest W / P that a launch may use for a given length (shared-memory bound).
 template <typename T> int max_lines_per_block(int n, bool col);
 // Default W (col) or P (row) for length n; `divisor` must be divisible by it.
 template <typename T> int default_lines_per_block(int n, bool col, int divisor);
+
+// 1D stage passes (ptf_kern1d.cu): nblk blocks of P solve pairs; mode is a
+// stepper stage (COL_RK4_*, COL_ETD_*) or COL_FWD_N (N into xout).
+template <typename T>
+cudaError_t launch_line1d(int nx, int mode, const Line1DArgs<T>& a, int P, int nblk, cudaStream_t st);
+template <typename T> int line1d_tpl(int nx);  // threads per solve pair
 
 // Element conversions (ptf_util.cu).
 template <typename T> cudaError_t launch_real_in(const double* src, T* dst, long long n, double scale, cudaStream_t st);

@@ -14,9 +14,9 @@ PTF_FOR_SIZES(PTF_EXTERN)
 #undef PTF_EXTERN
 
 template <typename T>
-cudaError_t launch_col(int n, const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st) {
+cudaError_t launch_col(int n, const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st, int carve) {
   switch (n) {
-#define PTF_CASE(n) case n: return PassLaunch<T, n>::col(a, W, nbx, batch, st);
+#define PTF_CASE(n) case n: return PassLaunch<T, n>::col(a, W, nbx, batch, st, carve);
     PTF_FOR_SIZES(PTF_CASE)
 #undef PTF_CASE
     default: return cudaErrorInvalidValue;
@@ -40,9 +40,9 @@ template <typename T> int max_lines_per_block(int n, bool col) {
     default: return 1;
   }
 }
-template <typename T> static int tpl_of(int n) {
+template <typename T> static int tpl_of(int n, bool col) {
   switch (n) {
-#define PTF_CASE(v) case v: return pass_tpl<T, v>();
+#define PTF_CASE(v) case v: return col ? col_tpl<T, v>() : pass_tpl<T, v>();
     PTF_FOR_SIZES(PTF_CASE)
 #undef PTF_CASE
     default: return 1;
@@ -53,7 +53,7 @@ template <typename T> static int tpl_of(int n) {
 // more, smaller blocks balance 152 SMs better).  Row pass: enough pairs for
 // >= 64 threads.  `divisor` must be divisible by the result.
 template <typename T> int default_lines_per_block(int n, bool col, int divisor) {
-  const int tpl = tpl_of<T>(n);
+  const int tpl = tpl_of<T>(n, col);
   const int mx = max_lines_per_block<T>(n, col);
   int m;
   if (col) {
@@ -68,8 +68,8 @@ template <typename T> int default_lines_per_block(int n, bool col, int divisor) 
   return m < 1 ? 1 : m;
 }
 
-template cudaError_t launch_col<float>(int, const ColArgs<float>&, int, int, int, cudaStream_t);
-template cudaError_t launch_col<double>(int, const ColArgs<double>&, int, int, int, cudaStream_t);
+template cudaError_t launch_col<float>(int, const ColArgs<float>&, int, int, int, cudaStream_t, int);
+template cudaError_t launch_col<double>(int, const ColArgs<double>&, int, int, int, cudaStream_t, int);
 template cudaError_t launch_row<float>(int, const RowArgs<float>&, int, int, int, cudaStream_t);
 template cudaError_t launch_row<double>(int, const RowArgs<double>&, int, int, int, cudaStream_t);
 template int max_lines_per_block<float>(int, bool);

@@ -4,6 +4,10 @@
 #pragma once
 #include "ptf_internal.h"
 
+#ifndef PTF_COL_CSTRIDE
+#define PTF_COL_CSTRIDE 1
+#endif
+
 namespace ptf {
 
 template <typename T, int N> struct PassLaunch {
@@ -15,28 +19,42 @@ template <typename T, int N> struct PassLaunch {
     if (cudaFuncGetAttributes(&at, kern) != cudaSuccess) return 0;
     return at.maxThreadsPerBlock;
   }
-  template <int MODE> static cudaError_t col_m(const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st) {
-    if (W * pass_tpl<T, N>() > max_threads(col_pass_kernel<T, N, MODE>)) return cudaErrorInvalidConfiguration;
-    const size_t smem = col_smem_bytes<T, N>(W);
-    cudaError_t e = cudaFuncSetAttribute(col_pass_kernel<T, N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  template <int MODE, int CS>
+  static cudaError_t col_k(const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st, int carve) {
+    auto kern = col_pass_kernel<T, N, MODE, CS>;
+    if (W * col_tpl<T, N>() > max_threads(kern)) return cudaErrorInvalidConfiguration;
+    const size_t smem = col_smem_bytes<T, N>(W, !col_reloads(MODE));
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, carve < 0 ? -1 : carve);
     if (e != cudaSuccess) return e;
-    col_pass_kernel<T, N, MODE><<<dim3(nbx, batch), dim3(W * pass_tpl<T, N>()), smem, st>>>(a);
+    kern<<<dim3(nbx, batch), dim3(W * col_tpl<T, N>()), smem, st>>>(a);
     return cudaGetLastError();
   }
-  static cudaError_t col(const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st) {
+  // Square grids (the row pitch equals square_pitch<N>) take the kernel with
+  // the pitch compiled in; others the runtime-stride kernel.
+  template <int MODE>
+  static cudaError_t col_m(const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st, int carve) {
+#if PTF_COL_CSTRIDE
+    constexpr bool stage = MODE >= COL_RK4_1 && MODE <= COL_ETD_4;
+    if (a.stride == square_pitch<N>() && (!stage || a.tplane == (long long)N * square_pitch<N>()))
+      return col_k<MODE, square_pitch<N>()>(a, W, nbx, batch, st, carve);
+#endif
+    return col_k<MODE, 0>(a, W, nbx, batch, st, carve);
+  }
+  static cudaError_t col(const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st, int carve = -1) {
     switch (a.mode) {
-      case COL_PROLOGUE: return col_m<COL_PROLOGUE>(a, W, nbx, batch, st);
-      case COL_FWD_STORE: return col_m<COL_FWD_STORE>(a, W, nbx, batch, st);
-      case COL_FWD_N: return col_m<COL_FWD_N>(a, W, nbx, batch, st);
-      case COL_RK4_1: return col_m<COL_RK4_1>(a, W, nbx, batch, st);
-      case COL_RK4_2: return col_m<COL_RK4_2>(a, W, nbx, batch, st);
-      case COL_RK4_3: return col_m<COL_RK4_3>(a, W, nbx, batch, st);
-      case COL_RK4_4: return col_m<COL_RK4_4>(a, W, nbx, batch, st);
-      case COL_ETD_1: return col_m<COL_ETD_1>(a, W, nbx, batch, st);
-      case COL_ETD_2: return col_m<COL_ETD_2>(a, W, nbx, batch, st);
-      case COL_ETD_3: return col_m<COL_ETD_3>(a, W, nbx, batch, st);
-      case COL_ETD_4: return col_m<COL_ETD_4>(a, W, nbx, batch, st);
-      case COL_YINV3: return col_m<COL_YINV3>(a, W, nbx, batch, st);
+      case COL_PROLOGUE: return col_m<COL_PROLOGUE>(a, W, nbx, batch, st, carve);
+      case COL_FWD_STORE: return col_m<COL_FWD_STORE>(a, W, nbx, batch, st, carve);
+      case COL_FWD_N: return col_m<COL_FWD_N>(a, W, nbx, batch, st, carve);
+      case COL_RK4_1: return col_m<COL_RK4_1>(a, W, nbx, batch, st, carve);
+      case COL_RK4_2: return col_m<COL_RK4_2>(a, W, nbx, batch, st, carve);
+      case COL_RK4_3: return col_m<COL_RK4_3>(a, W, nbx, batch, st, carve);
+      case COL_RK4_4: return col_m<COL_RK4_4>(a, W, nbx, batch, st, carve);
+      case COL_ETD_1: return col_m<COL_ETD_1>(a, W, nbx, batch, st, carve);
+      case COL_ETD_2: return col_m<COL_ETD_2>(a, W, nbx, batch, st, carve);
+      case COL_ETD_3: return col_m<COL_ETD_3>(a, W, nbx, batch, st, carve);
+      case COL_ETD_4: return col_m<COL_ETD_4>(a, W, nbx, batch, st, carve);
+      case COL_YINV3: return col_m<COL_YINV3>(a, W, nbx, batch, st, carve);
       default: return cudaErrorInvalidValue;
     }
   }
@@ -65,7 +83,7 @@ template <typename T, int N> int max_lines_n(bool col) {
   const size_t lb = col ? col_smem_bytes<T, N>(1) : row_smem_bytes<T, N>(1, 2);
   (void)sizeof(C);
   int m = (int)((200u * 1024u) / lb);
-  const int tpl = pass_tpl<T, N>();
+  const int tpl = col ? col_tpl<T, N>() : pass_tpl<T, N>();
   // the ETDRK4 stage-1 kernel carries the most state: it bounds every mode
   const int mt = col ? PassLaunch<T, N>::max_threads(col_pass_kernel<T, N, COL_ETD_1>)
                      : PassLaunch<T, N>::max_threads(row_pass_kernel<T, N>);

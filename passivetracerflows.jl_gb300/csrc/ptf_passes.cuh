@@ -147,10 +147,32 @@ __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefe
 // Dynamic shared memory of a column-pass block with W lines: the W FFT
 // lines, then a private slot array holding each thread's values between
 // transforms.
-template <typename T, int N> __host__ __device__ constexpr size_t col_smem_bytes(int W) {
-  return (size_t)W * (line_stride(N) + N) * sizeof(typename cplx_of<T>::type);
+// Column-pass variant: the modes whose next stage input is also written to
+// global memory (state or stage input) re-read it from there for the two
+// inverse transforms instead of parking it in shared memory.
+#ifndef PTF_COL_RELOAD
+#define PTF_COL_RELOAD 0
+#endif
+__host__ __device__ constexpr bool col_reloads(int mode) {
+  return PTF_COL_RELOAD && (mode == COL_PROLOGUE || mode == COL_FWD_STORE || mode == COL_RK4_1 ||
+                            mode == COL_RK4_2 || mode == COL_RK4_3 || mode == COL_RK4_4 || mode == COL_ETD_1 ||
+                            mode == COL_ETD_4);
 }
+// Shared memory of a column-pass block of W lines: the FFT lines, plus the
+// parking slots of the next stage input unless the mode re-reads it.
+template <typename T, int N> __host__ __device__ constexpr size_t col_smem_bytes(int W, bool park = true) {
+  return (size_t)W * (line_stride(N) + (park ? N : 0)) * sizeof(typename cplx_of<T>::type);
+}
+// Values per thread of the column pass (may differ from the row pass's: the
+// column pass is bound by latency, the row pass by shared-memory traffic).
+#ifndef PTF_COL_E_F32
+#define PTF_COL_E_F32 16
+#endif
+template <typename T, int N> struct ColE { static constexpr int value = PassE<T, N>::value; };
+template <int N> struct ColE<float, N> { static constexpr int value = N >= 256 ? PTF_COL_E_F32 : PassE<float, N>::value; };
+// threads per line: row pass (pass_tpl) and column pass (col_tpl)
 template <typename T, int N> __host__ __device__ constexpr int pass_tpl() { return N / PassE<T, N>::value; }
+template <typename T, int N> __host__ __device__ constexpr int col_tpl() { return N / ColE<T, N>::value; }
 
 // Compensated FP64 sum of the real parts of column 0 of a column-pass block
 // (lines w = 0: threads t*W, registers v[0..E)), returned in thread 0.  Uses
@@ -185,15 +207,108 @@ __device__ __forceinline__ double column0_sum(const C* v, int w, int t, C* line0
   return tot;
 }
 
+// Stepper stage combination at one spectral element o (FourierFlows RK4;
+// Cox-Matthews ETDRK4 with coefficient planes E, E2, zeta, alpha, beta,
+// gamma at cf[o + e*plane]).  Nh = the RHS transform N(stage input) here;
+// returns the next stage input (or the new state after stage 4) and updates
+// the state arrays S (sol), SI (stage input / ETDRK4 a), AC (accumulator),
+// N1p (ETDRK4 N(sol)).  RK4 stores only when `store` (batched slots); Lf()
+// gives the linear operator at o.
+template <typename T, int MODE, typename C, typename LF>
+__device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S, C* __restrict__ SI,
+                                           C* __restrict__ AC, C* __restrict__ N1p, const T* __restrict__ cf,
+                                           size_t plane, T dt, bool store, LF&& Lf) {
+  C x;
+  if (MODE == COL_RK4_1) {
+    const T L = Lf();
+    const C s = S[o];
+    C k; k.x = L * s.x + Nh.x; k.y = L * s.y + Nh.y;
+    C ac; ac.x = s.x + (dt / 6) * k.x; ac.y = s.y + (dt / 6) * k.y;
+    x.x = s.x + (dt / 2) * k.x; x.y = s.y + (dt / 2) * k.y;
+    if (store) { AC[o] = ac; SI[o] = x; }
+  } else if (MODE == COL_RK4_2 || MODE == COL_RK4_3) {
+    const T L = Lf();
+    const C si = SI[o], s = S[o];
+    C ac = AC[o];
+    C k; k.x = L * si.x + Nh.x; k.y = L * si.y + Nh.y;
+    ac.x += (dt / 3) * k.x; ac.y += (dt / 3) * k.y;
+    const T h = (MODE == COL_RK4_2) ? dt / 2 : dt;
+    x.x = s.x + h * k.x; x.y = s.y + h * k.y;
+    if (store) { AC[o] = ac; SI[o] = x; }
+  } else if (MODE == COL_RK4_4) {
+    const T L = Lf();
+    const C si = SI[o], ac = AC[o];
+    C k; k.x = L * si.x + Nh.x; k.y = L * si.y + Nh.y;
+    x.x = ac.x + (dt / 6) * k.x; x.y = ac.y + (dt / 6) * k.y;
+    if (store) S[o] = x;
+  } else if (MODE == COL_ETD_1) {
+    const T Ee = cf[o], E2 = cf[o + plane], ze = cf[o + 2 * plane], al = cf[o + 3 * plane];
+    const C s = S[o];
+    N1p[o] = Nh;
+    C ac; ac.x = Ee * s.x + al * Nh.x; ac.y = Ee * s.y + al * Nh.y;
+    AC[o] = ac;
+    x.x = E2 * s.x + ze * Nh.x; x.y = E2 * s.y + ze * Nh.y;
+    SI[o] = x;
+  } else if (MODE == COL_ETD_2) {
+    const T E2 = cf[o + plane], ze = cf[o + 2 * plane], be = cf[o + 4 * plane];
+    const C s = S[o];
+    C ac = AC[o];
+    ac.x += 2 * be * Nh.x; ac.y += 2 * be * Nh.y;
+    AC[o] = ac;
+    x.x = E2 * s.x + ze * Nh.x; x.y = E2 * s.y + ze * Nh.y;
+  } else if (MODE == COL_ETD_3) {
+    const T E2 = cf[o + plane], ze = cf[o + 2 * plane], be = cf[o + 4 * plane];
+    const C s1 = SI[o], N1 = N1p[o];
+    C ac = AC[o];
+    ac.x += 2 * be * Nh.x; ac.y += 2 * be * Nh.y;
+    AC[o] = ac;
+    x.x = E2 * s1.x + ze * (2 * Nh.x - N1.x); x.y = E2 * s1.y + ze * (2 * Nh.y - N1.y);
+  } else {  // COL_ETD_4
+    const T ga = cf[o + 5 * plane];
+    const C ac = AC[o];
+    x.x = ac.x + ga * Nh.x; x.y = ac.y + ga * Nh.y;
+    S[o] = x;
+  }
+  return x;
+}
+
+// The stage combination of the (0,0[,0]) mode in FP64 (FP32 handles): q =
+// {s, stage input, acc, N1} of one solve, kc = {L, E, E2, zeta, alpha, beta,
+// gamma} at that mode, Nd = N there.  Returns the next stage input (the new
+// state after stage 4).  Same formulas as stage_combine.
+template <int MODE>
+__device__ __forceinline__ double k0_combine(double* q, const double* kc, double dd, double Nd) {
+  double xd = q[0];
+  if (MODE == COL_RK4_1) {
+    const double k = kc[0] * q[0] + Nd;
+    q[2] = q[0] + dd / 6 * k; xd = q[0] + dd / 2 * k; q[1] = xd;
+  } else if (MODE == COL_RK4_2 || MODE == COL_RK4_3) {
+    const double k = kc[0] * q[1] + Nd;
+    q[2] += dd / 3 * k; xd = q[0] + (MODE == COL_RK4_2 ? dd / 2 : dd) * k; q[1] = xd;
+  } else if (MODE == COL_RK4_4) {
+    const double k = kc[0] * q[1] + Nd;
+    xd = q[2] + dd / 6 * k; q[0] = xd;
+  } else if (MODE == COL_ETD_1) {
+    q[3] = Nd; q[2] = kc[1] * q[0] + kc[4] * Nd; xd = kc[2] * q[0] + kc[3] * Nd; q[1] = xd;
+  } else if (MODE == COL_ETD_2) {
+    q[2] += 2 * kc[5] * Nd; xd = kc[2] * q[0] + kc[3] * Nd;
+  } else if (MODE == COL_ETD_3) {
+    q[2] += 2 * kc[5] * Nd; xd = kc[2] * q[1] + kc[3] * (2 * Nd - q[3]);
+  } else if (MODE == COL_ETD_4) {
+    xd = q[2] + kc[6] * Nd; q[0] = xd;
+  }
+  return xd;  // COL_FWD_STORE: the seeded state
+}
+
 // Body of one column-pass block (tile = column tile index, blk = block of
 // fields).  BATCHED: flat columns run over the slots of a bucket, each
 // thread carries its own slot; the linear operator and dt come from the
 // slot's parameters, and inactive slots are not written.
-template <typename T, int N, int MODE, bool BATCHED>
+template <typename T, int N, int MODE, bool BATCHED, int CSTRIDE = 0>
 __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk, unsigned char* smem_raw) {
   typedef typename cplx_of<T>::type C;
   static_assert(!BATCHED || MODE < COL_ETD_1 || MODE >= COL_FWD_N, "the batched form runs RK4");
-  constexpr int E = PassE<T, N>::value;
+  constexpr int E = ColE<T, N>::value;
   constexpr int TPL = N / E;
   constexpr int LS = line_stride(N);
   constexpr int RF0 = FirstRadix<N, -1, E>::value;  // forward input pattern
@@ -205,7 +320,9 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
   const int W = blockDim.x / TPL;
   const int w = threadIdx.x % W, t = threadIdx.x / W;
   int col = tile * W + w;
-  const int stride = a.stride;
+  // CSTRIDE != 0: the row pitch known at compile time (square grids), so
+  // the per-register offsets below become immediate offsets of the loads
+  const int stride = CSTRIDE ? CSTRIDE : a.stride;
   size_t boff = (size_t)blk * (size_t)a.bstride;
   bool store = true;
   T dt = a.dt;
@@ -220,7 +337,9 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
     dt = a.slots[slot].dt;
     boff = (size_t)slot * (size_t)a.bstride;
   }
-  const size_t plane = (size_t)a.tplane;
+  // table plane: compile-time too for the stage modes of a square 2D grid
+  constexpr bool STAGE = MODE >= COL_RK4_1 && MODE <= COL_ETD_4;
+  const size_t plane = (CSTRIDE && STAGE) ? (size_t)N * CSTRIDE : (size_t)a.tplane;
   const size_t toff = a.tab_per_block ? (size_t)blk * plane : 0;
   C* line = sm + w * LS;
   C* park = sm + W * LS;  // slot i of this thread: park[i*blockDim + tid]
@@ -247,6 +366,7 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
   }
 #endif
   constexpr bool K0MODE = (MODE >= COL_RK4_1 && MODE <= COL_ETD_4) || MODE == COL_FWD_STORE;
+  constexpr bool RELOAD = col_reloads(MODE);
   const bool k0blk = !BATCHED && K0MODE && a.k0 != nullptr && tile == 0;  // uniform across the block
   double k0N = 0;
   C v[E];
@@ -299,93 +419,30 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
         x = Nh; if (store) S[o] = x;
       } else if (MODE == COL_FWD_N) {
         x = Nh; if (store) a.nout[boff + o] = Nh;
-      } else if (MODE == COL_RK4_1) {
-        const T L = Lval(Lt, o, i);
-        const C s = S[o];
-        C k; k.x = L * s.x + Nh.x; k.y = L * s.y + Nh.y;
-        C ac; ac.x = s.x + (dt / 6) * k.x; ac.y = s.y + (dt / 6) * k.y;
-        x.x = s.x + (dt / 2) * k.x; x.y = s.y + (dt / 2) * k.y;
-        if (store) { AC[o] = ac; SI[o] = x; }
-      } else if (MODE == COL_RK4_2 || MODE == COL_RK4_3) {
-        const T L = Lval(Lt, o, i);
-        const C si = SI[o], s = S[o];
-        C ac = AC[o];
-        C k; k.x = L * si.x + Nh.x; k.y = L * si.y + Nh.y;
-        ac.x += (dt / 3) * k.x; ac.y += (dt / 3) * k.y;
-        const T h = (MODE == COL_RK4_2) ? dt / 2 : dt;
-        x.x = s.x + h * k.x; x.y = s.y + h * k.y;
-        if (store) { AC[o] = ac; SI[o] = x; }
-      } else if (MODE == COL_RK4_4) {
-        const T L = Lval(Lt, o, i);
-        const C si = SI[o], ac = AC[o];
-        C k; k.x = L * si.x + Nh.x; k.y = L * si.y + Nh.y;
-        x.x = ac.x + (dt / 6) * k.x; x.y = ac.y + (dt / 6) * k.y;
-        if (store) S[o] = x;
-      } else if (MODE == COL_ETD_1) {
-        const T Ee = cf[o], E2 = cf[o + plane], ze = cf[o + 2 * plane], al = cf[o + 3 * plane];
-        const C s = S[o];
-        N1p[o] = Nh;
-        C ac; ac.x = Ee * s.x + al * Nh.x; ac.y = Ee * s.y + al * Nh.y;
-        AC[o] = ac;
-        x.x = E2 * s.x + ze * Nh.x; x.y = E2 * s.y + ze * Nh.y;
-        SI[o] = x;
-      } else if (MODE == COL_ETD_2) {
-        const T E2 = cf[o + plane], ze = cf[o + 2 * plane], be = cf[o + 4 * plane];
-        const C s = S[o];
-        C ac = AC[o];
-        ac.x += 2 * be * Nh.x; ac.y += 2 * be * Nh.y;
-        AC[o] = ac;
-        x.x = E2 * s.x + ze * Nh.x; x.y = E2 * s.y + ze * Nh.y;
-      } else if (MODE == COL_ETD_3) {
-        const T E2 = cf[o + plane], ze = cf[o + 2 * plane], be = cf[o + 4 * plane];
-        const C s1 = SI[o], N1 = N1p[o];
-        C ac = AC[o];
-        ac.x += 2 * be * Nh.x; ac.y += 2 * be * Nh.y;
-        AC[o] = ac;
-        x.x = E2 * s1.x + ze * (2 * Nh.x - N1.x); x.y = E2 * s1.y + ze * (2 * Nh.y - N1.y);
-      } else {  // COL_ETD_4
-        const T ga = cf[o + 5 * plane];
-        const C ac = AC[o];
-        x.x = ac.x + ga * Nh.x; x.y = ac.y + ga * Nh.y;
-        S[o] = x;
+      } else {
+        x = stage_combine<T, MODE>(Nh, o, S, SI, AC, N1p, cf, plane, dt, store, [&]() { return Lval(Lt, o, i); });
       }
       if (k0thr && i == 0) {
         // the (0,0) mode in FP64: {s, stage input, acc, N1} of this solve
         double* q = a.k0 + (size_t)blk * 4;
         const double* kc = a.k0c;
         const double dd = a.dt64, Nd = k0N;
-        double xd = q[0];
-        if (MODE == COL_FWD_STORE) {
-          xd = q[0];
-        } else if (MODE == COL_RK4_1) {
-          const double k = kc[0] * q[0] + Nd;
-          q[2] = q[0] + dd / 6 * k; xd = q[0] + dd / 2 * k; q[1] = xd;
-        } else if (MODE == COL_RK4_2 || MODE == COL_RK4_3) {
-          const double k = kc[0] * q[1] + Nd;
-          q[2] += dd / 3 * k; xd = q[0] + (MODE == COL_RK4_2 ? dd / 2 : dd) * k; q[1] = xd;
-        } else if (MODE == COL_RK4_4) {
-          const double k = kc[0] * q[1] + Nd;
-          xd = q[2] + dd / 6 * k; q[0] = xd;
-        } else if (MODE == COL_ETD_1) {
-          q[3] = Nd; q[2] = kc[1] * q[0] + kc[4] * Nd; xd = kc[2] * q[0] + kc[3] * Nd; q[1] = xd;
-        } else if (MODE == COL_ETD_2) {
-          q[2] += 2 * kc[5] * Nd; xd = kc[2] * q[0] + kc[3] * Nd;
-        } else if (MODE == COL_ETD_3) {
-          q[2] += 2 * kc[5] * Nd; xd = kc[2] * q[1] + kc[3] * (2 * Nd - q[3]);
-        } else {  // COL_ETD_4
-          xd = q[2] + kc[6] * Nd; q[0] = xd;
-        }
+        const double xd = k0_combine<MODE>(q, kc, dd, Nd);
         x.x = (T)xd; x.y = 0;
         if (MODE == COL_FWD_STORE || MODE == COL_RK4_4 || MODE == COL_ETD_4) S[o] = x;
+        if (RELOAD && (MODE == COL_RK4_1 || MODE == COL_RK4_2 || MODE == COL_RK4_3 || MODE == COL_ETD_1)) SI[o] = x;
       }
-      park[i * nthr + threadIdx.x] = x;
+      if (!RELOAD) park[i * nthr + threadIdx.x] = x;
     }
   }
   if (MODE == COL_FWD_N || !a.do_inverse) return;  // uniform across the block
 
+  // where the next stage input is re-read from (RELOAD modes)
+  const C* __restrict__ X = (MODE == COL_RK4_1 || MODE == COL_RK4_2 || MODE == COL_RK4_3 || MODE == COL_ETD_1)
+                                ? a.si + boff : a.s + boff;
   // A = F^-1(s_next)
 #pragma unroll
-  for (int i = 0; i < E; ++i) v[i] = park[i * nthr + threadIdx.x];
+  for (int i = 0; i < E; ++i) v[i] = RELOAD ? X[PTF_OFF(RF, i)] : park[i * nthr + threadIdx.x];
   fft_line<N, +1, E>(v, t, line, a.tw);
   if (store) {
     C* __restrict__ Ap = a.A + boff;
@@ -399,7 +456,7 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
 #pragma unroll
   for (int i = 0; i < E; ++i) {
     const T k = kval<T, N>(reg_pos<N, RI, E>(t, i), BATCHED ? a.slots[slot].dky : a.dk);
-    const C x = park[i * nthr + threadIdx.x];
+    const C x = RELOAD ? X[PTF_OFF(RF, i)] : park[i * nthr + threadIdx.x];
     v[i].x = -k * x.y;
     v[i].y = k * x.x;
   }
@@ -423,11 +480,13 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
 #undef PTF_OFF
 }
 
-template <typename T, int N, int MODE>
+template <typename T, int N, int MODE, int CSTRIDE = 0>
 __global__ void __launch_bounds__(ColBounds<T>::threads, ColBounds<T>::blocks) col_pass_kernel(ColArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  col_body<T, N, MODE, false>(a, blockIdx.x, blockIdx.y, smem_raw);
+  col_body<T, N, MODE, false, CSTRIDE>(a, blockIdx.x, blockIdx.y, smem_raw);
 }
+// Row pitch of a square grid's half spectrum (nx/2 + 1 rounded up to 8).
+template <int N> __host__ __device__ constexpr int square_pitch() { return ((N / 2 + 1 + 7) / 8) * 8; }
 
 // ---------------------------------------------------------------------------
 // Row pass.  blockDim.x = P * (NX/E); pair pr = tid / (NX/E) handles rows

@@ -66,9 +66,9 @@ cudaError_t launch_spec_out(const typename cplx_of<T>::type* src, double2* dst, 
 
 // ---------------------------------------------------------------------------
 // FP64 k = 0 mode helpers.  Per-solve sums run as kSumBlocks blocks per solve
-// writing FP64 partials, then one warp per solve adding the partials with a
-// compensated (Kahan) sum.  FP64 inputs also use compensated per-thread sums;
-// FP32 values are exact in FP64, so a plain FP64 accumulation suffices.
+// writing FP64 partials (plain FP64 accumulation per thread over a short
+// strided run, then a block tree), then one warp per solve adding the
+// partials with a compensated (Kahan) sum.
 // ---------------------------------------------------------------------------
 constexpr int kSumBlocks = 64;
 
@@ -85,11 +85,19 @@ __global__ void __launch_bounds__(256) solve_partials_kernel(const Tin* __restri
   const long long chunk = (n + kSumBlocks - 1) / kSumBlocks;
   const long long lo = blockIdx.x * chunk, hi = lo + chunk < n ? lo + chunk : n;
   const Tin* xs = x + b * n;
-  double s = 0, c = 0;
-  for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-    if (sizeof(Tin) == sizeof(double)) kahan_add(s, c, (double)xs[i]);
-    else s += (double)xs[i];
+  // four independent FP64 accumulators per thread (each covers a few dozen
+  // values: error ~ count * eps64), then compensated sums across threads
+  double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+  const long long step = blockDim.x;
+  long long i = lo + threadIdx.x;
+  for (; i + 3 * step < hi; i += 4 * step) {
+    a0 += (double)xs[i];
+    a1 += (double)xs[i + step];
+    a2 += (double)xs[i + 2 * step];
+    a3 += (double)xs[i + 3 * step];
   }
+  for (; i < hi; i += step) a0 += (double)xs[i];
+  double s = (a0 + a1) + (a2 + a3);
   for (int off = 16; off > 0; off /= 2) s += __shfl_xor_sync(0xffffffffu, s, off);
   __shared__ double ws[8];
   if ((threadIdx.x & 31) == 0) ws[threadIdx.x / 32] = s;
@@ -139,18 +147,20 @@ cudaError_t launch_k0_to_spec(double2* dst, long long per_solve, int batch, cons
 // dst = src + (k0[4b] - sums[b]) / n for solve b: the field's sum becomes the
 // FP64 (0,0) mode.
 template <typename T>
-__global__ void real_out_shift_kernel(const T* __restrict__ src, double* __restrict__ dst, long long n, int batch,
+__global__ void real_out_shift_kernel(const T* __restrict__ src, double* __restrict__ dst, long long n,
                                       const double* __restrict__ k0, const double* __restrict__ sums) {
-  const long long tot = n * batch;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
-    const long long b = i / n;
-    dst[i] = (double)src[i] + (k0[4 * b] - sums[b]) / (double)n;
-  }
+  const long long b = blockIdx.y;  // solve
+  const double shift = (k0[4 * b] - sums[b]) / (double)n;
+  const T* s = src + b * n;
+  double* d = dst + b * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    d[i] = (double)s[i] + shift;
 }
 template <typename T>
 cudaError_t launch_real_out_shift(const T* src, double* dst, long long n, int batch, const double* k0,
                                   const double* sums, cudaStream_t st) {
-  real_out_shift_kernel<T><<<grid_for(n * batch), 256, 0, st>>>(src, dst, n, batch, k0, sums);
+  const int gx = (grid_for(n * batch) + batch - 1) / batch;
+  real_out_shift_kernel<T><<<dim3(gx < 1 ? 1 : gx, batch), 256, 0, st>>>(src, dst, n, k0, sums);
   return cudaGetLastError();
 }
 

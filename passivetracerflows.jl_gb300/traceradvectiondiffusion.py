@@ -32,7 +32,7 @@ from . import _lib as L
 
 __all__ = [
     "CPU", "GPU", "noflow", "OneDAdvectingFlow", "TwoDAdvectingFlow", "ThreeDAdvectingFlow",
-    "TwoDGrid", "ThreeDGrid", "gridpoints", "Problem", "set_c", "updatevars", "stepforward",
+    "OneDGrid", "TwoDGrid", "ThreeDGrid", "gridpoints", "Problem", "set_c", "updatevars", "stepforward",
 ]
 
 
@@ -86,17 +86,21 @@ class _Grid:
     def __init__(self, dim, nx, Lx, ny=None, Ly=None, nz=None, Lz=None):
         self.dim = dim
         self.nx, self.Lx = int(nx), float(Lx)
-        self.ny = int(ny if ny is not None else nx)
-        self.Ly = float(Ly if Ly is not None else Lx)
+        self.ny = int(ny if ny is not None else nx) if dim >= 2 else 1
+        self.Ly = float(Ly if Ly is not None else Lx) if dim >= 2 else 0.0
         self.nz = int(nz if nz is not None else nx) if dim == 3 else 1
         self.Lz = float(Lz if Lz is not None else Lx) if dim == 3 else 0.0
-        self.dx, self.dy = self.Lx / self.nx, self.Ly / self.ny
+        self.dx = self.Lx / self.nx
         self.x = -self.Lx / 2 + self.dx * np.arange(self.nx)
-        self.y = -self.Ly / 2 + self.dy * np.arange(self.ny)
         self.nkr = self.nx // 2 + 1
         self.kr = 2 * np.pi / self.Lx * np.arange(self.nkr)
-        self.l = 2 * np.pi / self.Ly * np.fft.fftfreq(self.ny, 1.0 / self.ny)
-        if dim == 3:
+        if dim >= 2:
+            self.dy = self.Ly / self.ny
+            self.y = -self.Ly / 2 + self.dy * np.arange(self.ny)
+            self.l = 2 * np.pi / self.Ly * np.fft.fftfreq(self.ny, 1.0 / self.ny)
+        if dim == 1:
+            self.shape = (self.nx,)
+        elif dim == 3:
             self.dz = self.Lz / self.nz
             self.z = -self.Lz / 2 + self.dz * np.arange(self.nz)
             self.m = 2 * np.pi / self.Lz * np.fft.fftfreq(self.nz, 1.0 / self.nz)
@@ -108,9 +112,16 @@ class _Grid:
 
     @property
     def Krsq(self):
+        if self.dim == 1:
+            return self.kr ** 2
         if self.dim == 3:
             return self.kr[None, None, :] ** 2 + self.l[None, :, None] ** 2 + self.m[:, None, None] ** 2
         return self.kr[None, :] ** 2 + self.l[:, None] ** 2
+
+
+def OneDGrid(dev=None, *, nx, Lx):
+    """FourierFlows ``OneDGrid(dev; nx, Lx)`` (host-side description)."""
+    return _Grid(1, nx, Lx)
 
 
 def TwoDGrid(dev=None, *, nx, Lx, ny=None, Ly=None):
@@ -124,12 +135,19 @@ def ThreeDGrid(dev=None, *, nx, Lx, ny=None, Ly=None, nz=None, Lz=None):
 
 
 def gridpoints(grid: _Grid):
-    """FourierFlows ``gridpoints(grid)``: full coordinate arrays, x fastest."""
+    """FourierFlows ``gridpoints(grid)``: full coordinate arrays, x fastest (1D: x)."""
+    if grid.dim == 1:
+        return grid.x.copy()
     if grid.dim == 3:
         Z, Y, X = np.meshgrid(grid.z, grid.y, grid.x, indexing="ij")
         return X, Y, Z
     Y, X = np.meshgrid(grid.y, grid.x, indexing="ij")
     return X, Y
+
+
+def _pts_tuple(grid):
+    p = gridpoints(grid)
+    return (p,) if grid.dim == 1 else p
 
 
 @dataclass
@@ -261,7 +279,7 @@ class Problem:
         self.vars = Vars(np.zeros(shape))
         self.clock = Clock(self)
         if flow.steadyflow:
-            pts = gridpoints(self.grid)
+            pts = _pts_tuple(self.grid)
             comps = (flow.u, flow.v, flow.w)[:dim]
             self.set_flow_arrays(*[_eval_on_grid(f, self.grid.shape, pts) for f in comps])
         else:
@@ -300,7 +318,7 @@ class Problem:
         t = self.clock.t
         if self._flow_t == t:
             return
-        pts = gridpoints(self.grid)
+        pts = _pts_tuple(self.grid)
         comps = (self.flow.u, self.flow.v, self.flow.w)[: self.grid.dim]
         self.set_flow_arrays(*[_eval_on_grid(f, self.grid.shape, pts, t) for f in comps])
         self._flow_t = t
@@ -320,7 +338,7 @@ class Problem:
         L.check(L.load().ptf_set_sol(self._h, a.ctypes.data_as(ct.c_void_p), L.PTF_HOST), self._h)
 
     def calcN(self, sol):
-        """The ``calcN!`` plugin (``:756-786``): ``N = rfft(-(u·∇c))`` for ``sol``."""
+        """The ``calcN!`` plugin (``:744-786``): ``N = rfft(-(u·∇c))`` for ``sol``."""
         shape = ((self.batch,) if self.batch > 1 else ()) + self.grid.spec_shape
         a = np.ascontiguousarray(np.broadcast_to(np.asarray(sol, dtype=np.complex128), shape))
         out = np.empty(shape, dtype=np.complex128)
@@ -338,7 +356,7 @@ class Problem:
                 self._h)
 
     _TUNING_FIELDS = ("col_lines", "col_lines_y", "row_pairs", "branches", "solves_per_group", "row_staged",
-                      "ms_per_step")
+                      "col_carveout", "ms_per_step")
 
     @property
     def tuning(self):

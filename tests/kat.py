@@ -29,6 +29,49 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(a), np.linalg.norm(b)))
 
 
+def _x1(api, prob):
+    x = _pts(api, prob)
+    return x[0] if isinstance(x, tuple) else x
+
+
+def constvel1D(api, dev, stepper="RK4", dt=1e-2, nsteps=40):
+    """test_constvel1D (:8-33): a Gaussian carried by u = 0.05 on 128 points."""
+    uvel, s = 0.05, 0.1
+    prob = _make(api, dev, api.OneDAdvectingFlow(u=lambda x: uvel), nx=128, Lx=2 * np.pi, κ=0.0, dt=dt,
+                 stepper=stepper)
+    x = _x1(api, prob)
+    f = lambda x: 0.1 * np.exp(-x ** 2 / (2 * s ** 2))
+    api.set_c(prob, f(x)); api.stepforward(prob, nsteps); api.updatevars(prob)
+    return _rel(f(x - uvel * nsteps * dt), prob.vars.c), 128 * nsteps * 1e-12
+
+
+def timedependentvel1D(api, dev, stepper="RK4", dt=0.002, tfinal=0.1, uvel=0.05):
+    """test_timedependentvel1D (:42-72): u(t) = uvel t + uvel dt/2, frozen at clock.t per step."""
+    nsteps = round(tfinal / dt)
+    flow = api.OneDAdvectingFlow(u=lambda x, t: uvel * t + uvel * dt / 2, steadyflow=False)
+    prob = _make(api, dev, flow, nx=128, Lx=2 * np.pi, κ=0.0, dt=dt, stepper=stepper)
+    x = _x1(api, prob)
+    s = 0.2
+    f = lambda x: 0.1 * np.exp(-x ** 2 / (2 * s ** 2))
+    api.set_c(prob, f(x)); api.stepforward(prob, nsteps); api.updatevars(prob)
+    tf = nsteps * dt
+    return _rel(f(x - 0.5 * uvel * tf ** 2), prob.vars.c), 128 * nsteps * 1e-12
+
+
+def diffusion1D(api, dev, stepper="RK4", dt=0.005, tfinal=0.1, steadyflow=True):
+    """test_diffusion1D (:232-262): heat kernel with variance 2 kappa t + 0.1 (the
+    reference's sigma(t)^2), amplitude 0.1 / sigma(t)."""
+    nsteps = round(tfinal / dt)
+    κ = 0.01
+    prob = _make(api, dev, api.OneDAdvectingFlow(steadyflow=steadyflow), nx=128, Lx=2 * np.pi, κ=κ, dt=dt,
+                 stepper=stepper)
+    x = _x1(api, prob)
+    sig = lambda t: np.sqrt(2 * κ * t + 0.1)
+    f = lambda x, t: (0.1 / sig(t)) * np.exp(-x ** 2 / (2 * sig(t) ** 2))
+    api.set_c(prob, f(x, 0.0)); api.stepforward(prob, nsteps); api.updatevars(prob)
+    return _rel(f(x, nsteps * dt), prob.vars.c), 128 * nsteps * 1e-12
+
+
 def constvel2D(api, dev, stepper="RK4", dt=1e-2, nsteps=40):
     """test_constvel2D (:79-106)."""
     nx, Lx, uvel, vvel = 128, 2 * np.pi, 0.2, 0.1

@@ -71,11 +71,23 @@ def test_create_rejects_bad_arguments(pkg, field, value, msg):
     assert msg in lib.ptf_last_error(None).decode()
 
 
-def test_create_rejects_unbuilt_dimension(pkg):
+@pytest.mark.parametrize("dim", [0, 4])
+def test_create_rejects_bad_dimension(pkg, dim):
     from ptf_gb300 import _lib as L
-    lib, c = _cfg(pkg, dim=1)
+    lib, c = _cfg(pkg, dim=dim)
     h = ct.c_void_p()
-    assert lib.ptf_create(ct.byref(c), ct.byref(h)) == L.PTF_ERR_UNSUPPORTED
+    assert lib.ptf_create(ct.byref(c), ct.byref(h)) == L.PTF_ERR_ARG
+    assert "dim must be 1, 2 or 3" in lib.ptf_last_error(None).decode()
+
+
+def test_create_1d_ignores_ny_nz(pkg):
+    """1D problems validate nx and Lx only (ny, nz, Ly, Lz are ignored): with no
+    GPU here the call gets past argument checking and fails at the device."""
+    from ptf_gb300 import _lib as L
+    lib, c = _cfg(pkg, dim=1, ny=3, nz=5, Ly=-1.0)
+    h = ct.c_void_p()
+    rc = lib.ptf_create(ct.byref(c), ct.byref(h))
+    assert rc != L.PTF_ERR_ARG
 
 
 def test_null_handle_calls_fail_cleanly(pkg):

@@ -17,6 +17,19 @@ def test_reference_kat_2d_gpu(gpu, name, tight, stepper):
     assert err <= tight
 
 
+@pytest.mark.parametrize("name,tight", [("constvel1D", 1e-9), ("timedependentvel1D", 1e-9), ("diffusion1D", 1e-9)])
+@pytest.mark.parametrize("stepper", ["RK4", "ETDRK4"])
+def test_reference_kat_1d_gpu(gpu, name, tight, stepper):
+    err, rtol = getattr(kat, name)(gpu, gpu.GPU(), stepper=stepper)
+    assert err <= rtol, f"{name}: {err:.3e} > reference rtol {rtol:.3e}"
+    assert err <= tight
+
+
+def test_diffusion1D_timevarying_gpu(gpu):
+    err, rtol = kat.diffusion1D(gpu, gpu.GPU(), steadyflow=False)
+    assert err <= rtol and err <= 1e-9
+
+
 def test_diffusion2D_timevarying_gpu(gpu):
     err, rtol = kat.diffusion2D(gpu, gpu.GPU(), steadyflow=False)
     assert err <= rtol and err <= 1e-9

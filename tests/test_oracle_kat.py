@@ -20,6 +20,18 @@ def test_reference_kat_2d(oracle, name, tight):
     assert err <= tight
 
 
+@pytest.mark.parametrize("name,tight", [("constvel1D", 1e-9), ("timedependentvel1D", 1e-9), ("diffusion1D", 1e-9)])
+def test_reference_kat_1d(oracle, name, tight):
+    err, rtol = getattr(kat, name)(oracle, None)
+    assert err <= rtol, f"{name}: {err:.3e} > reference rtol {rtol:.3e}"
+    assert err <= tight
+
+
+def test_diffusion1D_timevarying(oracle):
+    err, rtol = kat.diffusion1D(oracle, None, steadyflow=False)
+    assert err <= rtol and err <= 1e-9
+
+
 def test_diffusion2D_timevarying(oracle):
     err, rtol = kat.diffusion2D(oracle, None, steadyflow=False)
     assert err <= rtol and err <= 1e-9
