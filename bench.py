@@ -99,6 +99,21 @@ def initial_conditions(n, batch, seed):
     return out
 
 
+def profiled_traffic(kernel, precision, n, batch):
+    """DRAM bytes per launch of `kernel` measured by ncu (dram__bytes_read.sum +
+    dram__bytes_write.sum), as recorded in a summary under profiles/ by a line
+    ``traffic-per-launch: <kernel> <precision> n=<n> batch=<batch> bytes=<B>``."""
+    import re
+    pat = re.compile(r"traffic-per-launch:\s+(\S+)\s+(\S+)\s+n=(\d+)\s+batch=(\d+)\s+bytes=(\d+)")
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        for line in f.read_text().splitlines():
+            m = pat.search(line)
+            if m and m.group(1) == kernel and m.group(2) == precision and int(m.group(3)) == n \
+                    and int(m.group(4)) == batch:
+                return int(m.group(5)), f.name
+    return None, None
+
+
 def load_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -480,9 +495,12 @@ def run_ours(args):
     dom = max(prof, key=lambda k: prof[k]["ms"])
     d = prof[dom]
     achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9
+    traffic, traffic_src = profiled_traffic(dom, "f32", n, B)
     roof = {"bound": "hbm", "kernel": f"{dom} (FP32, {n}x{n}, batch {B})", "achieved": achieved, "peak": hbm_peak,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm_peak,
-            "traffic": None, "avg_launch_us": 1e3 * d["ms"] / max(1, d["launches"]),
+            "traffic": traffic, "traffic_source": traffic_src,
+            "traffic_over_algorithmic": (traffic / (d["bytes"] / max(1, d["launches"]))) if traffic else None,
+            "avg_launch_us": 1e3 * d["ms"] / max(1, d["launches"]),
             "algorithmic_bytes_per_launch": d["bytes"] / max(1, d["launches"]),
             "share_of_step": d["ms"] / sum(x["ms"] for x in prof.values())}
     passes = {k: {"ms_per_launch": x["ms"] / max(1, x["launches"]), "GBps": x["bytes"] / (x["ms"] / 1e3) / 1e9,
