@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=40.0, help="Poisson arrival rate (requests/s)")
     ap.add_argument("--ensemble-steps", type=int, default=100)
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes (no ptf_autotune)")
+    ap.add_argument("--acc-time", type=float, default=0.1, help="simulated time of the accuracy window")
     ap.add_argument("--no-comparator", action="store_true", help="skip the torch/cuFFT comparator")
     ap.add_argument("--profile-case", action="store_true",
                     help="only step the batched workload (for ncu); prints no result line")
@@ -365,7 +366,6 @@ def run_ours(args):
         prof[name] = {"ms": ms, "launches": cnt, "bytes": by}
     lib.ptf_profile(p32._h, 0)
     p32.tuning = {k: v for k, v in tuning32.items() if k != "ms_per_step"}
-    steps32 = W + 2 * K
     # ---------------- FP64 plain ----------------
     p64 = pkg.Problem(pkg.GPU(), pkg.TwoDAdvectingFlow(u=u, v=v), T=np.float64, batch=1, **kw)
     pkg.set_c(p64, c0[0])
@@ -394,28 +394,33 @@ def run_ours(args):
         ms, cnt, by = ct_read(lib, p64._h, kind)
         prof64[name] = {"ms": ms, "launches": cnt, "bytes": by}
     lib.ptf_profile(p64._h, 0)
-    steps64 = W + K64 + 8
     clocks = sampler.stop()
     # ---------------- accuracy vs the FP64 oracle ----------------
+    # The bench's own problems, restarted from the initial condition and
+    # stepped over a fixed window (t = 0.1 at dt = 5e-4): beyond it the
+    # flow's strain has thinned the tracer below the grid scale (the
+    # workload notes), and every solution, FP64 included, is dominated by
+    # under-resolution, not by the arithmetic.
     acc = {}
-    pkg.updatevars(p32)
-    pkg.updatevars(p64)
-    c32 = p32.vars.c[0].copy()
-    c64 = p64.vars.c.copy()
     if rank == 0 and not args.no_oracle_check:
         o = oracle_module()
-        # continue the FP64 GPU solve to the FP32 solve's step count, then compare both with the oracle
-        pkg.stepforward(p64, steps32 - steps64)
+        nacc = int(round(args.acc_time / dt))
+        pkg.set_c(p32, c0)
+        pkg.stepforward(p32, nacc)
+        pkg.updatevars(p32)
+        pkg.set_c(p64, c0[0])
+        pkg.stepforward(p64, nacc)
         pkg.updatevars(p64)
+        c32 = p32.vars.c[0].copy()
         c64 = p64.vars.c.copy()
         po = oracle_problem(o, n, dt)
         o.set_c(po, c0[0])
         t0 = time.perf_counter()
-        o.stepforward(po, steps32)
+        o.stepforward(po, nacc)
         o.updatevars(po)
         m0 = float(c0[0].sum())
         acc = {
-            "steps": steps32,
+            "steps": nacc, "t": nacc * dt,
             "rel_l2_fp32_vs_oracle": o.rel_l2(c32, po.vars.c),
             "rel_l2_fp64_vs_oracle": o.rel_l2(c64, po.vars.c),
             "mass_drift_fp32": float(c32.sum()) / m0 - 1,

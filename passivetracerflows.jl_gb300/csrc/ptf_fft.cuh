@@ -52,8 +52,9 @@ template <typename C> __device__ __forceinline__ C cmul_plain(C a, C b) {
   r.y = a.x * b.y + a.y * b.x;
   return r;
 }
-// FP32 radix-16 stages load w^1, w^2, w^4, w^8 of a butterfly's twiddles and
-// multiply out the rest (1): fewer table loads and far fewer live registers.
+// FP32 stages of radix >= 8 load the power-of-two powers of a butterfly's
+// twiddle and multiply out the rest (1): fewer table loads and far fewer
+// live registers.
 #ifndef PTF_TW_POW2
 #define PTF_TW_POW2 1
 #endif
@@ -193,11 +194,14 @@ template <int DIR, typename C> struct DFT<32, DIR, C> {
 
 constexpr int FFT_E = 16;  // default complex values per thread
 
-// Values per thread of the pass kernels: FP32 uses 32 (radix-32 stages:
-// fewer shared-memory exchanges, and its register file allows it); FP64
-// uses 16 (twice the register bytes per value).
+// Values per thread of the row (and 1D, batched) passes: 16; FP32 lengths
+// from PTF_ROW_E32_MIN on take 32 (radix-32 stages: fewer shared-memory
+// exchanges, at twice the registers per thread).
+#ifndef PTF_ROW_E32_MIN
+#define PTF_ROW_E32_MIN 0x7fffffff  // lengths from which FP32 row passes take 32 values per thread
+#endif
 template <typename T, int N> struct PassE { static constexpr int value = 16; };
-template <int N> struct PassE<float, N> { static constexpr int value = 16; };
+template <int N> struct PassE<float, N> { static constexpr int value = N >= PTF_ROW_E32_MIN ? 32 : 16; };
 
 // Radix schedule for N with E = 16: NB16 radix-16 stages plus one radix
 // REM stage (REM = 1 means none).  Forward order puts REM last; inverse
@@ -233,16 +237,22 @@ __device__ __forceinline__ void stage_compute(C* v, int t, const C* __restrict__
     const int j = t + q * (N / E);
     if (NS > 1) {
       const int k = j % NS;
-      if (PTF_TW_POW2 && R == 16 && sizeof(v[0].x) == 4) {
-        // FP32: load w^1, w^2, w^4, w^8 and form the other powers by at most
-        // three products (error a few ulp), a quarter of the table loads
+      if (PTF_TW_POW2 && R >= 8 && sizeof(v[0].x) == 4) {
+        // FP32: load the power-of-two powers w^1, w^2, w^4, ... of this
+        // butterfly's twiddle and form each other power as w^hb * w^(r-hb)
+        // (hb the highest power of two in r): at most log2(R)-1 products
+        // (error a few ulp), log2(R) table loads instead of R-1
         const int b = k * (N / (NS * R));
-        C w[16];
-        w[1] = ldtw(tw, b); w[2] = ldtw(tw, 2 * b); w[4] = ldtw(tw, 4 * b); w[8] = ldtw(tw, 8 * b);
-        w[3] = cmul_plain(w[2], w[1]);
-        w[5] = cmul_plain(w[4], w[1]); w[6] = cmul_plain(w[4], w[2]); w[7] = cmul_plain(w[4], w[3]);
+        C w[R];
 #pragma unroll
-        for (int r = 9; r < 16; ++r) w[r] = cmul_plain(w[8], w[r - 8]);
+        for (int p = 1; p < R; p *= 2) w[p] = ldtw(tw, p * b);
+#pragma unroll
+        for (int r = 3; r < R; ++r) {
+          if ((r & (r - 1)) == 0) continue;
+          int hb = 1;
+          while (hb * 2 <= r) hb *= 2;
+          w[r] = cmul_plain(w[hb], w[r - hb]);
+        }
 #pragma unroll
         for (int r = 1; r < R; ++r) v[q * R + r] = cmul_tw<DIR>(v[q * R + r], w[r]);
       } else {
