@@ -275,6 +275,29 @@ def dist_setup():
     return world, rank, local
 
 
+# Replicas (one process per GPU, no data-path collective): every rank steps
+# its own batch of independent solves from its own seed; the only collectives
+# are the barrier around the timed region and the max of the ranks' times.
+def replica_seed(rank, base=1234):
+    return base + rank
+
+
+def max_over_ranks(x, world, device):
+    """Largest value of x over the ranks (the job's time is its slowest rank's)."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, units_per_rank, seconds_max):
+    """Whole-job throughput: the units all ranks processed over the slowest rank's time."""
+    return world * units_per_rank / seconds_max
+
+
 def run_reference(args):
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -326,15 +349,10 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    def max_ranks(x):
+        return max_over_ranks(x, world, "cuda")
 
-    c0 = initial_conditions(n, B, 1234 + rank)
+    c0 = initial_conditions(n, B, replica_seed(rank))
     # ---------------- FP32 batched ----------------
     p32 = pkg.Problem(pkg.GPU(), pkg.TwoDAdvectingFlow(u=u, v=v), T=np.float32, batch=B, **kw)
     pkg.set_c(p32, c0)
@@ -352,9 +370,9 @@ def run_ours(args):
     e1.record(st32)
     e1.synchronize()
     barrier()
-    ms32 = max_over_ranks(e0.elapsed_time(e1))
+    ms32 = max_ranks(e0.elapsed_time(e1))
     launches = p32.kernel_launches - launches0
-    value = world * B * n * n * K / (ms32 / 1e3)
+    value = job_rate(world, B * n * n * K, ms32 / 1e3)
     # per-pass roofline (CUDA events around each pass; one branch, so that
     # the events of concurrent passes do not overlap)
     p32.tuning = dict(branches=1, solves_per_group=0)
@@ -385,7 +403,7 @@ def run_ours(args):
             b.record(st64)
             evs.append((a, b))
     torch.cuda.synchronize()
-    ms64 = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs))
+    ms64 = max_ranks(sum(a.elapsed_time(b) for a, b in evs))
     value64 = world * n * n * K64 / (ms64 / 1e3)
     lib.ptf_profile(p64._h, 1)
     pkg.stepforward(p64, 8)
@@ -470,8 +488,8 @@ def run_ours(args):
         pkg.stepforward(p32, S)
         pkg.updatevars(p32)
     t1 = time.perf_counter()
-    e2e_s = max_over_ranks(t1 - t0)
-    e2e_val = world * B * n * n * frames * S / e2e_s
+    e2e_s = max_ranks(t1 - t0)
+    e2e_val = job_rate(world, B * n * n * frames * S, e2e_s)
     bytes_field = B * n * n * 8
     # ---------------- other configurations (rank 0, bounded) ----------------
     configs = {}

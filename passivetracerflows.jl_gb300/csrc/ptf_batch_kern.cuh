@@ -43,6 +43,21 @@ template <typename T> size_t batch_smem_bytes() {
 
 constexpr unsigned long long kSpinLimit = 1ull << 24;  // x 128 ns sleeps: about 2 s
 
+// The bodies of one work item as real calls: the item loop of the persistent
+// kernel then holds few values across an item, and each body gets the
+// registers it needs instead of competing with hoisted loop state.
+template <typename T, int N>
+__device__ __noinline__ void batch_row_item(const RowArgs<T>* ra, T stage_c, int local, unsigned char* smem) {
+  RowArgs<T> a = *ra;
+  a.stage_c = stage_c;
+  row_body<T, N, true>(a, local, 0, smem);
+}
+template <typename T, int N, int MODE>
+__device__ __noinline__ void batch_col_item(const ColArgs<T>* ca, int local, unsigned char* smem) {
+  // buckets hold square grids: the row pitch is square_pitch<N>()
+  col_body<T, N, MODE, true, square_pitch<N>()>(*ca, local, 0, smem);
+}
+
 template <typename T, int MODE>
 __global__ void __launch_bounds__(kBatchThreads, BatchBounds<T>::blocks)
 batch_stage_kernel(const BatchPlan<T>* __restrict__ plan, unsigned int* ctr, int* err, T stage_c) {
@@ -57,11 +72,9 @@ batch_stage_kernel(const BatchPlan<T>* __restrict__ plan, unsigned int* ctr, int
     if (item < row_total) {
       int b = 0;
       while (b + 1 < nb && item >= plan->b[b + 1].row_begin) ++b;
-      RowArgs<T> ra = plan->b[b].row;
-      ra.stage_c = stage_c;
       const int local = item - plan->b[b].row_begin;
       switch (plan->b[b].n) {
-#define PTF_CASE(n) case n: row_body<T, n, true>(ra, local, 0, smem); break;
+#define PTF_CASE(n) case n: batch_row_item<T, n>(&plan->b[b].row, stage_c, local, smem); break;
         PTF_BATCH_SIZES(PTF_CASE)
 #undef PTF_CASE
         default: break;
@@ -85,10 +98,9 @@ batch_stage_kernel(const BatchPlan<T>* __restrict__ plan, unsigned int* ctr, int
       }
       __syncthreads();
       if (s_ok) {
-        ColArgs<T> ca = plan->b[b].col;
         const int local = item - plan->b[b].col_begin;
         switch (plan->b[b].n) {
-#define PTF_CASE(n) case n: col_body<T, n, MODE, true>(ca, local, 0, smem); break;
+#define PTF_CASE(n) case n: batch_col_item<T, n, MODE>(&plan->b[b].col, local, smem); break;
           PTF_BATCH_SIZES(PTF_CASE)
 #undef PTF_CASE
           default: break;
