@@ -293,7 +293,7 @@ double pass_bytes(const ptf_handle* h, int kind, int mode) {
       case COL_RK4_4: return B * 3 * M + Tb + P;
       case COL_ETD_1: return B * 4 * M + 4 * Tb + P;
       case COL_ETD_2: return B * 5 * M + 3 * Tb + P;
-      case COL_ETD_3: return B * 6 * M + 3 * Tb + P;
+      case COL_ETD_3: return B * 5 * M + 2 * Tb + P;
       default: return B * 3 * M + Tb + P;  // COL_ETD_4
     }
   }
@@ -310,9 +310,9 @@ double pass_bytes(const ptf_handle* h, int kind, int mode) {
     case COL_RK4_1: return B * 6 * M + Tb;
     case COL_RK4_2: case COL_RK4_3: return B * 8 * M + Tb;
     case COL_RK4_4: return B * 6 * M + Tb;
-    case COL_ETD_1: return B * 7 * M + 4 * Tb;
+    case COL_ETD_1: return B * 6 * M + 4 * Tb;
     case COL_ETD_2: return B * 6 * M + 3 * Tb;
-    case COL_ETD_3: return B * 7 * M + 3 * Tb;
+    case COL_ETD_3: return B * 6 * M + 2 * Tb;
     default: return B * 5 * M + Tb;  // COL_ETD_4
   }
 }
@@ -527,12 +527,12 @@ int auto_group(const ptf_handle* h) {
 template <typename T> int enqueue_step(ptf_handle* h, int group) {
   const bool etd = h->cfg.stepper == PTF_ETDRK4;
   if (h->dim == 1) {
-    // stage inputs: RK4 s, si, si, si (si updated in place); ETDRK4 s, a (si),
-    // b (A), c (A, in place)
+    // stage inputs: RK4 s, si, si, si (si updated in place); ETDRK4 s, then
+    // a, b, c in A (updated in place)
     int rc;
     if (etd) {
-      if ((rc = run_line1d<T>(h, COL_ETD_1, h->s, nullptr))) return rc;
-      if ((rc = run_line1d<T>(h, COL_ETD_2, h->si, h->A))) return rc;
+      if ((rc = run_line1d<T>(h, COL_ETD_1, h->s, h->A))) return rc;
+      if ((rc = run_line1d<T>(h, COL_ETD_2, h->A, h->A))) return rc;
       if ((rc = run_line1d<T>(h, COL_ETD_3, h->A, h->A))) return rc;
       return run_line1d<T>(h, COL_ETD_4, h->A, nullptr);
     }
@@ -1017,7 +1017,6 @@ int ptf_create(const ptf_config* cfg, ptf_handle** out) {
   const size_t sp = (size_t)h->nphys * B * elem_r(h);
   bool ok = true;
   ok = ok && dev_alloc(h, &h->s, sc) && dev_alloc(h, &h->si, sc) && dev_alloc(h, &h->acc, sc);
-  if (c.stepper == PTF_ETDRK4) ok = ok && dev_alloc(h, &h->n1, sc);
   ok = ok && dev_alloc(h, &h->A, sc);
   if (h->dim >= 2) ok = ok && dev_alloc(h, &h->B, sc);
   if (h->dim == 2) ok = ok && dev_alloc(h, &h->Nx, sc);

@@ -23,7 +23,7 @@ template <typename T, int N> struct PassLaunch {
   static cudaError_t col_k(const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st, int carve) {
     auto kern = col_pass_kernel<T, N, MODE, CS>;
     if (W * col_tpl<T, N>() > max_threads(kern)) return cudaErrorInvalidConfiguration;
-    const size_t smem = col_smem_bytes<T, N>(W, !col_reloads(MODE));
+    const size_t smem = col_smem_bytes<T, N>(W);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, carve < 0 ? -1 : carve);
     if (e != cudaSuccess) return e;

@@ -13,7 +13,7 @@ namespace ptf {
 template <typename T> struct Line1DArgs {
   typedef typename cplx_of<T>::type C;
   const C* xin;  // stage input, pitch complex per solve
-  C* xout;       // next stage input (ETDRK4 stages 2 and 3; may alias xin); N for COL_FWD_N
+  C* xout;       // next stage input (ETDRK4 stages 1-3; may alias xin); N for COL_FWD_N
   C *s, *si, *acc, *n1;
   const T* u;  // flow on the grid, pre-scaled by -1/(2 nx), shared by the batch
   const T* Ltab;
@@ -117,9 +117,10 @@ __global__ void __launch_bounds__(256) line1d_kernel(Line1DArgs<T> a) {
         const double xd = k0_combine<MODE>(q, a.k0c, a.dt64, (double)o[j].x);
         x.x = (T)xd; x.y = 0;
         if (MODE == COL_RK4_4 || MODE == COL_ETD_4) a.s[r] = x;
-        else if (MODE == COL_RK4_1 || MODE == COL_RK4_2 || MODE == COL_RK4_3 || MODE == COL_ETD_1) a.si[r] = x;
+        else if (MODE == COL_RK4_1 || MODE == COL_RK4_2 || MODE == COL_RK4_3) a.si[r] = x;
       }
-      if (MODE == COL_ETD_2 || MODE == COL_ETD_3) a.xout[r + k] = x;
+      // ETDRK4 stage inputs a, b, c go to xout (SI holds d = E2 a - zeta N(s))
+      if (MODE == COL_ETD_1 || MODE == COL_ETD_2 || MODE == COL_ETD_3) a.xout[r + k] = x;
     }
   }
 }

@@ -136,32 +136,14 @@ __device__ __forceinline__ T kval(int p, T dk) { return (T)(p < N / 2 ? p : p - 
 #ifndef PTF_COL_THREADS_F32
 #define PTF_COL_THREADS_F32 256
 #endif
-#ifndef PTF_PREFETCH
-#define PTF_PREFETCH 0
-#endif
 template <typename T> struct ColBounds { static constexpr int threads = 256, blocks = PTF_COL_MINB_F64; };
 template <> struct ColBounds<float> { static constexpr int threads = PTF_COL_THREADS_F32, blocks = PTF_COL_MINB_F32; };
 
-// Ask L2 to fetch a line now; the load that follows later finds it there.
-__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 // Dynamic shared memory of a column-pass block with W lines: the W FFT
-// lines, then a private slot array holding each thread's values between
-// transforms.
-// Column-pass variant: the modes whose next stage input is also written to
-// global memory (state or stage input) re-read it from there for the two
-// inverse transforms instead of parking it in shared memory.
-#ifndef PTF_COL_RELOAD
-#define PTF_COL_RELOAD 0
-#endif
-__host__ __device__ constexpr bool col_reloads(int mode) {
-  return PTF_COL_RELOAD && (mode == COL_PROLOGUE || mode == COL_FWD_STORE || mode == COL_RK4_1 ||
-                            mode == COL_RK4_2 || mode == COL_RK4_3 || mode == COL_RK4_4 || mode == COL_ETD_1 ||
-                            mode == COL_ETD_4);
-}
-// Shared memory of a column-pass block of W lines: the FFT lines, plus the
-// parking slots of the next stage input unless the mode re-reads it.
-template <typename T, int N> __host__ __device__ constexpr size_t col_smem_bytes(int W, bool park = true) {
-  return (size_t)W * (line_stride(N) + (park ? N : 0)) * sizeof(typename cplx_of<T>::type);
+// lines, then a private slot array holding each thread's next stage input
+// between the two inverse transforms.
+template <typename T, int N> __host__ __device__ constexpr size_t col_smem_bytes(int W) {
+  return (size_t)W * (line_stride(N) + N) * sizeof(typename cplx_of<T>::type);
 }
 // Values per thread of the column pass (may differ from the row pass's: the
 // column pass is bound by latency, the row pass by shared-memory traffic).
@@ -211,9 +193,9 @@ __device__ __forceinline__ double column0_sum(const C* v, int w, int t, C* line0
 // Cox-Matthews ETDRK4 with coefficient planes E, E2, zeta, alpha, beta,
 // gamma at cf[o + e*plane]).  Nh = the RHS transform N(stage input) here;
 // returns the next stage input (or the new state after stage 4) and updates
-// the state arrays S (sol), SI (stage input / ETDRK4 a), AC (accumulator),
-// N1p (ETDRK4 N(sol)).  RK4 stores only when `store` (batched slots); Lf()
-// gives the linear operator at o.
+// the state arrays S (sol), SI (RK4 stage input / ETDRK4 d = E2 a - zeta N(sol)),
+// AC (accumulator).  RK4 stores only when `store` (batched slots); Lf() gives
+// the linear operator at o.  (N1p is unused: kept for the call sites.)
 template <typename T, int MODE, typename C, typename LF>
 __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S, C* __restrict__ SI,
                                            C* __restrict__ AC, C* __restrict__ N1p, const T* __restrict__ cf,
@@ -242,13 +224,16 @@ __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S,
     x.x = ac.x + (dt / 6) * k.x; x.y = ac.y + (dt / 6) * k.y;
     if (store) S[o] = x;
   } else if (MODE == COL_ETD_1) {
+    // a = E2 s + zeta N(s) is the next input; stage 3's
+    // c = E2 a + zeta (2 N(b) - N(s)) = d + 2 zeta N(b) needs only
+    // d = E2 a - zeta N(s), stored in SI in place of a and N(s)
     const T Ee = cf[o], E2 = cf[o + plane], ze = cf[o + 2 * plane], al = cf[o + 3 * plane];
     const C s = S[o];
-    N1p[o] = Nh;
     C ac; ac.x = Ee * s.x + al * Nh.x; ac.y = Ee * s.y + al * Nh.y;
     AC[o] = ac;
     x.x = E2 * s.x + ze * Nh.x; x.y = E2 * s.y + ze * Nh.y;
-    SI[o] = x;
+    C d; d.x = E2 * x.x - ze * Nh.x; d.y = E2 * x.y - ze * Nh.y;
+    SI[o] = d;
   } else if (MODE == COL_ETD_2) {
     const T E2 = cf[o + plane], ze = cf[o + 2 * plane], be = cf[o + 4 * plane];
     const C s = S[o];
@@ -257,12 +242,12 @@ __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S,
     AC[o] = ac;
     x.x = E2 * s.x + ze * Nh.x; x.y = E2 * s.y + ze * Nh.y;
   } else if (MODE == COL_ETD_3) {
-    const T E2 = cf[o + plane], ze = cf[o + 2 * plane], be = cf[o + 4 * plane];
-    const C s1 = SI[o], N1 = N1p[o];
+    const T ze = cf[o + 2 * plane], be = cf[o + 4 * plane];
+    const C d = SI[o];
     C ac = AC[o];
     ac.x += 2 * be * Nh.x; ac.y += 2 * be * Nh.y;
     AC[o] = ac;
-    x.x = E2 * s1.x + ze * (2 * Nh.x - N1.x); x.y = E2 * s1.y + ze * (2 * Nh.y - N1.y);
+    x.x = d.x + 2 * ze * Nh.x; x.y = d.y + 2 * ze * Nh.y;
   } else {  // COL_ETD_4
     const T ga = cf[o + 5 * plane];
     const C ac = AC[o];
@@ -273,7 +258,7 @@ __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S,
 }
 
 // The stage combination of the (0,0[,0]) mode in FP64 (FP32 handles): q =
-// {s, stage input, acc, N1} of one solve, kc = {L, E, E2, zeta, alpha, beta,
+// {s, stage input (ETDRK4: d), acc, unused} of one solve, kc = {L, E, E2, zeta, alpha, beta,
 // gamma} at that mode, Nd = N there.  Returns the next stage input (the new
 // state after stage 4).  Same formulas as stage_combine.
 template <int MODE>
@@ -289,11 +274,11 @@ __device__ __forceinline__ double k0_combine(double* q, const double* kc, double
     const double k = kc[0] * q[1] + Nd;
     xd = q[2] + dd / 6 * k; q[0] = xd;
   } else if (MODE == COL_ETD_1) {
-    q[3] = Nd; q[2] = kc[1] * q[0] + kc[4] * Nd; xd = kc[2] * q[0] + kc[3] * Nd; q[1] = xd;
+    q[2] = kc[1] * q[0] + kc[4] * Nd; xd = kc[2] * q[0] + kc[3] * Nd; q[1] = kc[2] * xd - kc[3] * Nd;
   } else if (MODE == COL_ETD_2) {
     q[2] += 2 * kc[5] * Nd; xd = kc[2] * q[0] + kc[3] * Nd;
   } else if (MODE == COL_ETD_3) {
-    q[2] += 2 * kc[5] * Nd; xd = kc[2] * q[1] + kc[3] * (2 * Nd - q[3]);
+    q[2] += 2 * kc[5] * Nd; xd = q[1] + 2 * kc[3] * Nd;
   } else if (MODE == COL_ETD_4) {
     xd = q[2] + kc[6] * Nd; q[0] = xd;
   }
@@ -348,25 +333,7 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
   // offset of register i for a first/last stage of radix R
 #define PTF_OFF(R, i) (tb + (((i) / (R)) * TPL + ((i) % (R)) * (N / (R))) * stride)
 
-#if PTF_PREFETCH
-  // The stage combination reads state and tables only after the forward
-  // transform: start fetching them now so the transform hides the latency.
-  if (MODE >= COL_RK4_1 && MODE <= COL_ETD_4) {
-    const bool rk = MODE <= COL_RK4_4;
-#pragma unroll
-    for (int i = 0; i < E; ++i) {
-      const int o = PTF_OFF(RF, i);
-      if (MODE == COL_RK4_1 || MODE == COL_RK4_2 || MODE == COL_RK4_3 || MODE == COL_ETD_1 || MODE == COL_ETD_2)
-        prefetch_l2(a.s + boff + o);
-      if (MODE == COL_RK4_2 || MODE == COL_RK4_3 || MODE == COL_RK4_4 || MODE == COL_ETD_3) prefetch_l2(a.si + boff + o);
-      if (MODE != COL_RK4_1 && MODE != COL_ETD_1) prefetch_l2(a.acc + boff + o);
-      if (MODE == COL_ETD_3) prefetch_l2(a.n1 + boff + o);
-      if (rk && !BATCHED) prefetch_l2(a.Ltab + (size_t)(a.tab_per_block ? (size_t)blk * a.tplane : 0) + o);
-    }
-  }
-#endif
   constexpr bool K0MODE = (MODE >= COL_RK4_1 && MODE <= COL_ETD_4) || MODE == COL_FWD_STORE;
-  constexpr bool RELOAD = col_reloads(MODE);
   const bool k0blk = !BATCHED && K0MODE && a.k0 != nullptr && tile == 0;  // uniform across the block
   double k0N = 0;
   C v[E];
@@ -423,26 +390,22 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
         x = stage_combine<T, MODE>(Nh, o, S, SI, AC, N1p, cf, plane, dt, store, [&]() { return Lval(Lt, o, i); });
       }
       if (k0thr && i == 0) {
-        // the (0,0) mode in FP64: {s, stage input, acc, N1} of this solve
+        // the (0,0) mode in FP64: {s, stage input (ETDRK4: d), acc, -} of this solve
         double* q = a.k0 + (size_t)blk * 4;
         const double* kc = a.k0c;
         const double dd = a.dt64, Nd = k0N;
         const double xd = k0_combine<MODE>(q, kc, dd, Nd);
         x.x = (T)xd; x.y = 0;
         if (MODE == COL_FWD_STORE || MODE == COL_RK4_4 || MODE == COL_ETD_4) S[o] = x;
-        if (RELOAD && (MODE == COL_RK4_1 || MODE == COL_RK4_2 || MODE == COL_RK4_3 || MODE == COL_ETD_1)) SI[o] = x;
       }
-      if (!RELOAD) park[i * nthr + threadIdx.x] = x;
+      park[i * nthr + threadIdx.x] = x;
     }
   }
   if (MODE == COL_FWD_N || !a.do_inverse) return;  // uniform across the block
 
-  // where the next stage input is re-read from (RELOAD modes)
-  const C* __restrict__ X = (MODE == COL_RK4_1 || MODE == COL_RK4_2 || MODE == COL_RK4_3 || MODE == COL_ETD_1)
-                                ? a.si + boff : a.s + boff;
   // A = F^-1(s_next)
 #pragma unroll
-  for (int i = 0; i < E; ++i) v[i] = RELOAD ? X[PTF_OFF(RF, i)] : park[i * nthr + threadIdx.x];
+  for (int i = 0; i < E; ++i) v[i] = park[i * nthr + threadIdx.x];
   fft_line<N, +1, E>(v, t, line, a.tw);
   if (store) {
     C* __restrict__ Ap = a.A + boff;
@@ -456,7 +419,7 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
 #pragma unroll
   for (int i = 0; i < E; ++i) {
     const T k = kval<T, N>(reg_pos<N, RI, E>(t, i), BATCHED ? a.slots[slot].dky : a.dk);
-    const C x = RELOAD ? X[PTF_OFF(RF, i)] : park[i * nthr + threadIdx.x];
+    const C x = park[i * nthr + threadIdx.x];
     v[i].x = -k * x.y;
     v[i].y = k * x.x;
   }
@@ -632,24 +595,6 @@ __device__ __forceinline__ void row_body(const RowArgs<T>& a, int tile, int blk,
   const long long r0 = boff + (long long)yy0 * pitch, r1 = r0 + pitch;
   const long long q0 = (long long)yy0 * NX, q1 = q0 + NX;
 
-#if PTF_PREFETCH
-  // The flow rows and the second row's inputs are read after the first
-  // inverse transform: start fetching them now.
-  if (a.mode == ROW_RHS || a.mode == ROW_RHS3) {
-    const bool arrays = !BATCHED || a.slots[slot].flow_kind == FLOW_ARRAYS;
-#pragma unroll
-    for (int i = 0; i < E; ++i) {
-      const int x = reg_pos<NX, RIL, E>(t, i);
-      if (arrays) {
-        prefetch_l2(a.u + foff + q0 + x); prefetch_l2(a.v + foff + q0 + x);
-        prefetch_l2(a.u + foff + q1 + x); prefetch_l2(a.v + foff + q1 + x);
-      }
-      const int k = reg_pos<NX, RI0, E>(t, i);
-      const int kk = k <= NX / 2 ? k : NX - k;
-      prefetch_l2(a.A + r1 + kk); prefetch_l2(a.B + r1 + kk);
-    }
-  }
-#endif
 
   C v[E];
   if (a.mode == ROW_R2C) {
