@@ -120,7 +120,7 @@ struct ptf_handle {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   // device buffers (compute precision)
-  void *s = nullptr, *si = nullptr, *acc = nullptr, *n1 = nullptr;
+  void *s = nullptr, *si = nullptr, *acc = nullptr;
   void *A = nullptr, *B = nullptr, *Nx = nullptr;  // 2D; in 3D A = P1, Nx = P1
   void *C = nullptr;                               // 3D: P2 (Z2 / C)
   void *Ltab = nullptr, *coef = nullptr, *twx = nullptr, *twy = nullptr, *twz = nullptr;
@@ -135,7 +135,7 @@ struct ptf_handle {
   // schedule: solves per group (a step runs all its passes group by group so
   // a group's fields stay in L2), and a CUDA graph of one step
   int* err_dev = nullptr;  // device error flag of bounded waits
-  // FP64 k = 0 mode (FP32 handles): per solve {s, stage input, acc, N1} of
+  // FP64 k = 0 mode (FP32 handles): per solve {s, stage input (ETDRK4: d), acc, -} of
   // the (0,0[,0]) mode, then 64 sum partials per solve and one sum per
   // solve; k0c = FP64 {L, E, E2, zeta, alpha, beta, gamma} at (0,0[,0])
   bool k0mode = false;
@@ -369,7 +369,7 @@ template <typename T> int run_col(ptf_handle* h, const ColGeom& g, int mode, con
   std::memset(&a, 0, sizeof(a));
   a.nxin = goff<const C>(io.nxin, h, gr);
   a.s = goff<C>(io.s ? io.s : h->s, h, gr);
-  a.si = goff<C>(h->si, h, gr); a.acc = goff<C>(h->acc, h, gr); a.n1 = goff<C>(h->n1, h, gr);
+  a.si = goff<C>(h->si, h, gr); a.acc = goff<C>(h->acc, h, gr);
   a.A = goff<C>(io.A, h, gr); a.B = goff<C>(io.B, h, gr); a.Cout = goff<C>(io.Cout, h, gr);
   a.z2in = goff<const C>(io.z2in, h, gr); a.nout = goff<C>(io.nout, h, gr);
   a.tw = (const C*)(g.axis == 2 ? h->twz : h->twy);
@@ -438,7 +438,7 @@ template <typename T> int run_line1d(ptf_handle* h, int mode, const void* xin, v
   Line1DArgs<T> a;
   std::memset(&a, 0, sizeof(a));
   a.xin = (const C*)xin; a.xout = (C*)xout;
-  a.s = (C*)h->s; a.si = (C*)h->si; a.acc = (C*)h->acc; a.n1 = (C*)h->n1;
+  a.s = (C*)h->s; a.si = (C*)h->si; a.acc = (C*)h->acc;
   a.u = (const T*)h->u; a.Ltab = (const T*)h->Ltab; a.coef = (const T*)h->coef; a.tw = (const C*)h->twx;
   a.dkx = (T)(2 * M_PI / h->cfg.Lx);
   a.dt = (T)h->cfg.dt;

@@ -14,14 +14,14 @@ template <typename T> struct Line1DArgs {
   typedef typename cplx_of<T>::type C;
   const C* xin;  // stage input, pitch complex per solve
   C* xout;       // next stage input (ETDRK4 stages 1-3; may alias xin); N for COL_FWD_N
-  C *s, *si, *acc, *n1;
+  C *s, *si, *acc;
   const T* u;  // flow on the grid, pre-scaled by -1/(2 nx), shared by the batch
   const T* Ltab;
   const T* coef;
   const C* tw;
   T dkx, dt;
   int pitch, rows;  // rows = solves (even: an odd batch carries one zero solve)
-  // FP64 k = 0 mode (FP32 handles): per-solve {s, stage input, acc, N1}, coefficients
+  // FP64 k = 0 mode (FP32 handles): per-solve {s, stage input (ETDRK4: d), acc, -}, coefficients
   double* k0;
   const double* k0c;
   double dt64;
@@ -110,8 +110,8 @@ __global__ void __launch_bounds__(256) line1d_kernel(Line1DArgs<T> a) {
         a.xout[r + k] = o[j];
         continue;
       }
-      x = stage_combine<T, MODE>(o[j], k, a.s + r, a.si + r, a.acc + r, a.n1 ? a.n1 + r : nullptr, a.coef,
-                                 (size_t)pitch, a.dt, true, [&]() { return a.Ltab[k]; });
+      x = stage_combine<T, MODE>(o[j], k, a.s + r, a.si + r, a.acc + r, a.coef, (size_t)pitch, a.dt, true,
+                                 [&]() { return a.Ltab[k]; });
       if (a.k0 != nullptr && k == 0) {
         double* q = a.k0 + (size_t)(y0 + j) * 4;
         const double xd = k0_combine<MODE>(q, a.k0c, a.dt64, (double)o[j].x);

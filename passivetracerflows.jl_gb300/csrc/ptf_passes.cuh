@@ -59,9 +59,8 @@ template <typename T> struct ColArgs {
   typedef typename cplx_of<T>::type C;
   const C* nxin;   // forward input
   C* s;            // state (sol); COL_YINV3: the z-inverse Z1
-  C* si;           // RK4: current stage input; ETDRK4: sol1 ("a")
+  C* si;           // RK4: current stage input; ETDRK4: d = E2 a - zeta N(sol)
   C* acc;          // accumulator of the update
-  C* n1;           // ETDRK4: N(sol)
   C* A;            // F^-1(s_next)
   C* B;            // F^-1(i k s_next)
   C* Cout;         // COL_YINV3: F^-1(z2in)
@@ -82,7 +81,7 @@ template <typename T> struct ColArgs {
   const int* slot_list;
   int nslots, slot_cols;
   // FP64 k = 0 mode (FP32 handles, main column pass): per-solve FP64 state
-  // {s, stage input, acc, N1} of the (0,0[,0]) mode and its FP64
+  // {s, stage input (ETDRK4: d), acc, -} of the (0,0[,0]) mode and its FP64
   // coefficients {L, E, E2, zeta, alpha, beta, gamma}; null when off
   double* k0;
   const double* k0c;
@@ -195,10 +194,10 @@ __device__ __forceinline__ double column0_sum(const C* v, int w, int t, C* line0
 // returns the next stage input (or the new state after stage 4) and updates
 // the state arrays S (sol), SI (RK4 stage input / ETDRK4 d = E2 a - zeta N(sol)),
 // AC (accumulator).  RK4 stores only when `store` (batched slots); Lf() gives
-// the linear operator at o.  (N1p is unused: kept for the call sites.)
+// the linear operator at o.
 template <typename T, int MODE, typename C, typename LF>
 __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S, C* __restrict__ SI,
-                                           C* __restrict__ AC, C* __restrict__ N1p, const T* __restrict__ cf,
+                                           C* __restrict__ AC, const T* __restrict__ cf,
                                            size_t plane, T dt, bool store, LF&& Lf) {
   C x;
   if (MODE == COL_RK4_1) {
@@ -372,7 +371,6 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
     C* __restrict__ S = a.s + boff;
     C* __restrict__ SI = a.si + boff;
     C* __restrict__ AC = a.acc + boff;
-    C* __restrict__ N1p = a.n1 + boff;
     const T* __restrict__ Lt = a.Ltab + toff;
     const T* __restrict__ cf = a.coef + 6 * toff;
 #pragma unroll
@@ -387,7 +385,7 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
       } else if (MODE == COL_FWD_N) {
         x = Nh; if (store) a.nout[boff + o] = Nh;
       } else {
-        x = stage_combine<T, MODE>(Nh, o, S, SI, AC, N1p, cf, plane, dt, store, [&]() { return Lval(Lt, o, i); });
+        x = stage_combine<T, MODE>(Nh, o, S, SI, AC, cf, plane, dt, store, [&]() { return Lval(Lt, o, i); });
       }
       if (k0thr && i == 0) {
         // the (0,0) mode in FP64: {s, stage input (ETDRK4: d), acc, -} of this solve
