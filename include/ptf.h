@@ -43,7 +43,10 @@ enum ptf_status {
   PTF_ERR_MEMORY = 5       /* device memory budget exceeded */
 };
 
-enum ptf_stepper { PTF_RK4 = 0, PTF_ETDRK4 = 1 };
+/* FourierFlows steppers; the Filtered ones multiply the state by the
+ * FourierFlows spectral filter after every step (the MultiLayerQG-coupled
+ * Problem's default is FilteredRK4, src/traceradvectiondiffusion.jl:228). */
+enum ptf_stepper { PTF_RK4 = 0, PTF_ETDRK4 = 1, PTF_FILTERED_RK4 = 2, PTF_FILTERED_ETDRK4 = 3 };
 enum ptf_precision { PTF_FP64 = 0, PTF_FP32 = 1 };
 /* PTF_CLOCK_T evaluates a time-varying flow at clock.t for all four stages
  * of a step, as the reference does (src/traceradvectiondiffusion.jl:718,737);
@@ -91,6 +94,12 @@ const char* ptf_last_error(const ptf_handle* h);
  * ConstDiffSteadyFlowParams (:436-452).  Also used for a time-varying flow
  * re-evaluated by the caller at clock.t before each step (:715-718). */
 int ptf_set_flow_arrays(ptf_handle* h, const double* u, const double* v, const double* w, int32_t where);
+/* One flow per solve of a 2D batch -- the layers of the MultiLayerQG-coupled
+ * tracer (Problem(MQGprob), :225-250; calcN!, :788-804): solve j is advected
+ * by u_j + U[j], v_j, with u, v holding batch*nx*ny values (layer-major) and
+ * U batch values (host; NULL: zero).  Called before each step with the
+ * MultiLayerQG state's velocities, as calcN! reads MQGprob.vars.u, v. */
+int ptf_set_flow_layers(ptf_handle* h, const double* u, const double* v, const double* U, int32_t where);
 
 /* set_c!(prob, c) (:844-852, :872): sol = rfft(c). */
 int ptf_set_c(ptf_handle* h, const double* c, int32_t where);
@@ -133,7 +142,9 @@ int ptf_set_schedule(ptf_handle* h, int32_t solves_per_group, int32_t branches, 
  * row_staged: 2D RHS row pass staging its rows in shared memory with bulk
  * copies (falls back to the direct kernel where that does not fit);
  * col_carveout: the share of the SM's L1/shared storage the column passes
- * ask to be shared memory (the rest caches, among others, register spills);
+ * ask to be shared memory (the rest caches, among others, register spills;
+ * set by hand -- measured no better than the driver's choice, so the tuner
+ * leaves it at -1);
  * ms_per_step: the time measured by ptf_autotune (0 when not tuned).  Line
  * counts are powers of two dividing the lines of the pass, within the
  * block's resource limit.  Shapes do not change results. */

@@ -279,7 +279,47 @@ class ETDRK4:
         sol[...] = (self.E * sol + self.alpha * N1 + 2 * self.beta * (N2 + N3) + self.gamma * N4)
 
 
-STEPPERS = {"RK4": RK4, "ETDRK4": ETDRK4}
+def makefilter(g: Grid, order=4, innerK=0.65, outerK=1.0, tol=1e-15):
+    """FourierFlows' spectral filter (``makefilter``, used by its Filtered
+    steppers; FourierFlows is not in the reference tree, so this restates its
+    published form -- parity unpinned): ``K = |(kr dx, l dy[, m dz])| / pi``;
+    1 for ``K < innerK``, else ``exp(-decay (K - innerK)^order)`` with
+    ``decay = -log(tol) / (outerK - innerK)^order``."""
+    K2 = (g.kr * g.dx / np.pi) ** 2
+    if g.dim >= 2:
+        K2 = K2 + (g.l * g.dy / np.pi) ** 2
+    if g.dim >= 3:
+        K2 = K2 + (g.m * g.dz / np.pi) ** 2
+    K = np.broadcast_to(np.sqrt(K2), g.spec_shape)
+    decay = -np.log(tol) / (outerK - innerK) ** order
+    return np.where(K < innerK, 1.0, np.exp(-decay * np.clip(K - innerK, 0, None) ** order))
+
+
+class FilteredRK4(RK4):
+    """FourierFlows FilteredRK4: an RK4 step, then ``sol .*= filter``."""
+
+    def __init__(self, L, dt, g):
+        super().__init__(L, dt)
+        self.filter = makefilter(g)
+
+    def step(self, sol, clock, p, g):
+        super().step(sol, clock, p, g)
+        sol *= self.filter
+
+
+class FilteredETDRK4(ETDRK4):
+    """FourierFlows FilteredETDRK4: an ETDRK4 step, then ``sol .*= filter``."""
+
+    def __init__(self, L, dt, g):
+        super().__init__(L, dt)
+        self.filter = makefilter(g)
+
+    def step(self, sol, clock, p, g):
+        super().step(sol, clock, p, g)
+        sol *= self.filter
+
+
+STEPPERS = {"RK4": RK4, "ETDRK4": ETDRK4, "FilteredRK4": FilteredRK4, "FilteredETDRK4": FilteredETDRK4}
 
 
 # --------------------------------------------------------------------------
@@ -317,12 +357,57 @@ class Problem:
         if stepper not in STEPPERS:
             raise ValueError(f"unsupported stepper {stepper!r}")
         self.stepper_name = stepper
-        self.timestepper = STEPPERS[stepper](self.L, float(dt))
+        if stepper.startswith("Filtered"):
+            self.timestepper = STEPPERS[stepper](self.L, float(dt), g)
+        else:
+            self.timestepper = STEPPERS[stepper](self.L, float(dt))
 
     def set_flow_arrays(self, *vel):
         """Steady flow given directly as grid arrays (device-array flow input)."""
         self.params.ugrid = tuple(np.asarray(a, dtype=np.float64).reshape(self.grid.shape) for a in vel)
         self.params.steady = True
+
+
+class MultiLayerProblem:
+    """``Problem(MQGprob; κ, η, stepper="FilteredRK4")`` (``:225-250``): one 2D
+    tracer per layer with ``L = -κ kr² - η l²`` (``:556-566``), advected by
+    the layer's ``u + U_j``, ``v`` (``calcN!``, ``:788-804``).  The layer
+    velocities are set with ``set_layer_flows`` before each step (what
+    ``calcN!`` reads from ``MQGprob.vars``)."""
+
+    def __init__(self, *, nx, Lx=2 * np.pi, ny=None, Ly=None, nlayers, dt, kappa=0.1, eta=None,
+                 stepper="FilteredRK4"):
+        self.layers = [Problem(TwoDAdvectingFlow(), nx=nx, Lx=Lx, ny=ny, Ly=Ly, kappa=kappa, eta=eta, dt=dt,
+                               stepper=stepper) for _ in range(int(nlayers))]
+        self.nlayers = int(nlayers)
+        self.grid = self.layers[0].grid
+        self.clock = self.layers[0].clock
+
+    def set_layer_flows(self, u, v, U=None):
+        U = np.zeros(self.nlayers) if U is None else np.asarray(U, dtype=np.float64).reshape(self.nlayers)
+        for j, pr in enumerate(self.layers):
+            pr.set_flow_arrays(np.asarray(u[j]) + U[j], np.asarray(v[j]))
+
+    @property
+    def sol(self):
+        return np.stack([pr.sol for pr in self.layers])
+
+    @property
+    def c(self):
+        return np.stack([pr.vars.c for pr in self.layers])
+
+    def set_c(self, c):
+        for j, pr in enumerate(self.layers):
+            set_c(pr, np.asarray(c)[j])
+
+    def stepforward(self, nsteps=1):
+        for pr in self.layers:
+            stepforward(pr, nsteps)
+        self.clock = self.layers[0].clock
+
+    def updatevars(self):
+        for pr in self.layers:
+            updatevars(pr)
 
 
 def set_c(prob: Problem, c):

@@ -12,10 +12,11 @@ user API, as PassiveTracerFlows.jl re-exports ``TracerAdvectionDiffusion``
 from . import traceradvectiondiffusion as TracerAdvectionDiffusion
 from .traceradvectiondiffusion import (CPU, GPU, Problem, OneDAdvectingFlow, ThreeDAdvectingFlow,
                                        TwoDAdvectingFlow, ThreeDGrid, TwoDGrid, OneDGrid, gridpoints, noflow, set_c,
-                                       stepforward, updatevars)
+                                       stepforward, updatevars, MultiLayerQGFlow, MultiLayerTracerProblem)
 from ._lib import LIB_PATH, load as load_library
 from .batched import BatchedProblem, Server, SolveSpec
 
 __all__ = ["TracerAdvectionDiffusion", "CPU", "GPU", "Problem", "OneDAdvectingFlow", "TwoDAdvectingFlow",
            "ThreeDAdvectingFlow", "OneDGrid", "TwoDGrid", "ThreeDGrid", "gridpoints", "noflow", "set_c", "stepforward",
-           "updatevars", "LIB_PATH", "load_library", "BatchedProblem", "Server", "SolveSpec"]
+           "updatevars", "LIB_PATH", "load_library", "BatchedProblem", "Server", "SolveSpec", "MultiLayerQGFlow",
+           "MultiLayerTracerProblem"]

@@ -12,7 +12,7 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "libptf.so"
 
 PTF_OK, PTF_ERR_ARG, PTF_ERR_CUDA, PTF_ERR_STATE, PTF_ERR_UNSUPPORTED, PTF_ERR_MEMORY = 0, 1, 2, 3, 4, 5
-PTF_RK4, PTF_ETDRK4 = 0, 1
+PTF_RK4, PTF_ETDRK4, PTF_FILTERED_RK4, PTF_FILTERED_ETDRK4 = 0, 1, 2, 3
 PTF_FP64, PTF_FP32 = 0, 1
 PTF_CLOCK_T, PTF_STAGE_T = 0, 1
 PTF_HOST, PTF_DEVICE = 0, 1
@@ -133,6 +133,7 @@ SIGNATURES = {
     "ptf_server_wait_all": (ct.c_int, [ct.c_void_p, ct.c_double]),
     "ptf_server_get_stats": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfServerStats)]),
     "ptf_set_schedule": (ct.c_int, [ct.c_void_p, ct.c_int32, ct.c_int32, ct.c_int32]),
+    "ptf_set_flow_layers": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int32]),
     "ptf_get_tuning": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfTuning)]),
     "ptf_set_tuning": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfTuning)]),
     "ptf_autotune": (ct.c_int, [ct.c_void_p, ct.c_int32, ct.c_int32]),

@@ -117,13 +117,18 @@ struct ptf_handle {
   long long rows = 0;       // x rows per solve (nz*ny)
   int bpad = 1;             // solves held on the device: 1D rounds the batch up to pairs
   bool fp32 = false;
+  bool etd = false;         // ETDRK4 (plain or filtered)
+  bool filtered = false;    // Filtered steppers: the state is multiplied by `filt` after each step
+  bool flow_layers = false; // one flow per solve (ptf_set_flow_layers)
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   // device buffers (compute precision)
   void *s = nullptr, *si = nullptr, *acc = nullptr;
   void *A = nullptr, *B = nullptr, *Nx = nullptr;  // 2D; in 3D A = P1, Nx = P1
   void *C = nullptr;                               // 3D: P2 (Z2 / C)
-  void *Ltab = nullptr, *coef = nullptr, *twx = nullptr, *twy = nullptr, *twz = nullptr;
+  void *Ltab = nullptr, *coef = nullptr, *twx = nullptr, *twy = nullptr, *twz = nullptr, *filt = nullptr;
+  void *ul = nullptr, *vl = nullptr;  // per-solve flows (batch x nphys each)
+  double* layerU = nullptr;            // per-solve mean flow added to u (device, batch values)
   void *u = nullptr, *v = nullptr, *w = nullptr, *phys = nullptr;
   double* stage = nullptr;  // FP64 staging buffer
   long long stage_elems = 0;
@@ -235,7 +240,28 @@ template <typename T> int upload_tables(ptf_handle* h) {
                                     dt * ph[2], dt * ph[3], 0.0};
     if ((rc = upload(h, h->k0c, kc, "upload k = 0 coefficients"))) return rc;
   }
-  if (c.stepper == PTF_ETDRK4) {
+  if (h->filtered) {
+    // FourierFlows' spectral filter (makefilter: order 4, innerK 0.65,
+    // outerK 1, tol 1e-15): K = |(kr dx, l dy, m dz)| / pi; 1 below innerK,
+    // exp(-decay (K - innerK)^4) above, decay = -log(tol) / (outerK - innerK)^4
+    const double innerK = 0.65, outerK = 1.0, order = 4.0, tol = 1e-15;
+    const double decay = -std::log(tol) / std::pow(outerK - innerK, order);
+    const double dx = c.Lx / h->nx, dy = h->dim >= 2 ? c.Ly / h->ny : 0.0, dz = h->dim == 3 ? c.Lz / h->nz : 0.0;
+    std::vector<T> ft(plane, (T)0);
+    for (int q = 0; q < nz; ++q) {
+      const double m = h->dim == 3 ? (q < nz / 2 ? q : q - nz) * dkz : 0.0;
+      for (int j = 0; j < ny; ++j) {
+        const double l = h->dim == 1 ? 0.0 : (j < ny / 2 ? j : j - ny) * dky;
+        for (int k = 0; k < nkr; ++k) {
+          const double a = k * dkx * dx / M_PI, b = l * dy / M_PI, e = m * dz / M_PI;
+          const double K = std::sqrt(a * a + b * b + e * e);
+          ft[((size_t)q * ny + j) * pitch + k] = (T)(K < innerK ? 1.0 : std::exp(-decay * std::pow(K - innerK, order)));
+        }
+      }
+    }
+    if ((rc = upload(h, h->filt, ft, "upload filter"))) return rc;
+  }
+  if (h->etd) {
     std::vector<T> cf(6 * plane, (T)0);
     const double dt = c.dt;
     // L depends on l and m only through l^2 and m^2: compute rows j <= ny/2,
@@ -373,7 +399,7 @@ template <typename T> int run_col(ptf_handle* h, const ColGeom& g, int mode, con
   a.A = goff<C>(io.A, h, gr); a.B = goff<C>(io.B, h, gr); a.Cout = goff<C>(io.Cout, h, gr);
   a.z2in = goff<const C>(io.z2in, h, gr); a.nout = goff<C>(io.nout, h, gr);
   a.tw = (const C*)(g.axis == 2 ? h->twz : h->twy);
-  a.Ltab = (const T*)h->Ltab; a.coef = (const T*)h->coef;
+  a.Ltab = (const T*)h->Ltab; a.coef = (const T*)h->coef; a.filt = (const T*)h->filt;
   a.dt = (T)h->cfg.dt;
   a.dk = (T)g.dk;
   a.stride = g.stride; a.mode = mode; a.do_inverse = do_inverse ? 1 : 0;
@@ -404,6 +430,10 @@ int run_row(ptf_handle* h, int mode, const void* A, const void* B, const void* C
   a.A = goff<const C>(A, h, gr); a.B = goff<const C>(B, h, gr); a.Cin = goff<const C>(Cin, h, gr);
   a.out = goff<C>(out, h, gr);
   a.u = (const T*)h->u; a.v = (const T*)h->v; a.w = (const T*)h->w;
+  if (h->flow_layers) {  // one flow per solve: offset by the group, stride per field block
+    a.u = (const T*)h->ul + (size_t)gr.b0 * h->nphys;
+    a.v = (const T*)h->vl + (size_t)gr.b0 * h->nphys;
+  }
   a.cin = cin ? (const T*)cin + (size_t)gr.b0 * h->nphys : nullptr;
   a.cout = cout ? (T*)cout + (size_t)gr.b0 * h->nphys : nullptr;
   a.tw = (const C*)h->twx;
@@ -413,7 +443,7 @@ int run_row(ptf_handle* h, int mode, const void* A, const void* B, const void* C
   a.park_slots = h->dim == 3 ? 2 : 1;
   a.err = h->err_dev;
   a.tma = (h->row_tma && h->dim == 2 && mode == ROW_RHS) ? 1 : 0;
-  a.bstride = h->plane; a.pstride = h->nphys; a.fstride = 0;
+  a.bstride = h->plane; a.pstride = h->nphys; a.fstride = h->flow_layers ? h->nphys : 0;
   const int P = h->rowP;
   int nby = (int)((h->rows / 2) / P), nfields = gr.nb;
   if (h->dim == 1) {  // one row per solve: the pairs run over the (padded) batch
@@ -440,6 +470,7 @@ template <typename T> int run_line1d(ptf_handle* h, int mode, const void* xin, v
   a.xin = (const C*)xin; a.xout = (C*)xout;
   a.s = (C*)h->s; a.si = (C*)h->si; a.acc = (C*)h->acc;
   a.u = (const T*)h->u; a.Ltab = (const T*)h->Ltab; a.coef = (const T*)h->coef; a.tw = (const C*)h->twx;
+  a.filt = (const T*)h->filt;
   a.dkx = (T)(2 * M_PI / h->cfg.Lx);
   a.dt = (T)h->cfg.dt;
   a.pitch = h->pitch; a.rows = h->bpad;
@@ -510,7 +541,7 @@ int auto_group(const ptf_handle* h) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
   const double per = 7.0 * (double)h->plane * (double)elem_c(h);
-  const double shared = (double)h->plane * elem_r(h) * (h->cfg.stepper == PTF_ETDRK4 ? 7 : 1) +
+  const double shared = (double)h->plane * elem_r(h) * (h->etd ? 7 : 1) +
                         (double)h->nphys * elem_r(h) * h->dim;
   int g = (int)((0.75 * (double)l2 - shared) / per);
   (void)g;
@@ -525,7 +556,7 @@ int auto_group(const ptf_handle* h) {
 // fork from it and join back), so passes of different groups can run at the
 // same time; within a branch the groups follow one another.
 template <typename T> int enqueue_step(ptf_handle* h, int group) {
-  const bool etd = h->cfg.stepper == PTF_ETDRK4;
+  const bool etd = h->etd;
   if (h->dim == 1) {
     // stage inputs: RK4 s, si, si, si (si updated in place); ETDRK4 s, then
     // a, b, c in A (updated in place)
@@ -877,13 +908,9 @@ template <typename T> int autotune_impl(ptf_handle* h, int steps) {
   };
   if (!rc) rc = trial(best);
   // one knob at a time, starting from the best so far
-  for (int knob = 0; knob < 6 && !rc; ++knob) {
+  for (int knob = 0; knob < 5 && !rc; ++knob) {
     std::vector<ptf_tuning> cands;
-    if (knob == 5) {  // shared-memory carve-out of the column passes (L1 left for register spills)
-      if (h->dim >= 2)
-        for (int pct : {-1, 50, 60, 70, 80, 90, 100}) { ptf_tuning t = best; t.col_carveout = pct; cands.push_back(t); }
-    }
-    for (int v = 1; v <= 64 && knob < 5; v *= 2) {
+    for (int v = 1; v <= 64; v *= 2) {
       ptf_tuning t = best;
       if (knob == 0) { if (h->dim < 2 || !lines_ok(h, h->gmain.n, true, v, h->gmain.ncols)) continue; t.col_lines = v; }
       else if (knob == 1) { if (h->dim != 3 || !lines_ok(h, h->gy3.n, true, v, h->gy3.ncols)) continue; t.col_lines_y = v; }
@@ -967,7 +994,8 @@ int ptf_create(const ptf_config* cfg, ptf_handle** out) {
   if (!(c.Lx > 0) || (c.dim >= 2 && !(c.Ly > 0)) || (c.dim == 3 && !(c.Lz > 0)))
     return fail(nullptr, PTF_ERR_ARG, "domain lengths must be positive");
   if (!(c.dt > 0) || !std::isfinite(c.dt)) return fail(nullptr, PTF_ERR_ARG, "dt must be positive and finite");
-  if (c.stepper != PTF_RK4 && c.stepper != PTF_ETDRK4) return fail(nullptr, PTF_ERR_ARG, "stepper must be RK4 or ETDRK4");
+  if (c.stepper < PTF_RK4 || c.stepper > PTF_FILTERED_ETDRK4)
+    return fail(nullptr, PTF_ERR_ARG, "stepper must be RK4, ETDRK4, FilteredRK4 or FilteredETDRK4");
   if (c.precision != PTF_FP64 && c.precision != PTF_FP32) return fail(nullptr, PTF_ERR_ARG, "precision must be FP64 or FP32");
   if (c.time_mode != PTF_CLOCK_T && c.time_mode != PTF_STAGE_T) return fail(nullptr, PTF_ERR_ARG, "time_mode must be CLOCK_T or STAGE_T");
   if (c.batch < 1) return fail(nullptr, PTF_ERR_ARG, "batch must be >= 1");
@@ -982,6 +1010,8 @@ int ptf_create(const ptf_config* cfg, ptf_handle** out) {
   h->nx = c.nx; h->ny = c.dim >= 2 ? c.ny : 1; h->nz = c.dim == 3 ? c.nz : 1;
   h->bpad = c.dim == 1 ? c.batch + (c.batch & 1) : c.batch;
   h->fp32 = c.precision == PTF_FP32;
+  h->etd = c.stepper == PTF_ETDRK4 || c.stepper == PTF_FILTERED_ETDRK4;
+  h->filtered = c.stepper == PTF_FILTERED_RK4 || c.stepper == PTF_FILTERED_ETDRK4;
   h->k0mode = h->fp32 && c.k0_mode == 1;
   h->nkr = c.nx / 2 + 1;
   h->pitch = ((h->nkr + 7) / 8) * 8;
@@ -1022,7 +1052,8 @@ int ptf_create(const ptf_config* cfg, ptf_handle** out) {
   if (h->dim == 2) ok = ok && dev_alloc(h, &h->Nx, sc);
   else if (h->dim == 3) { ok = ok && dev_alloc(h, &h->C, sc); h->Nx = h->A; }
   ok = ok && dev_alloc(h, &h->Ltab, (size_t)h->plane * elem_r(h));
-  if (c.stepper == PTF_ETDRK4) ok = ok && dev_alloc(h, &h->coef, 6 * (size_t)h->plane * elem_r(h));
+  if (h->etd) ok = ok && dev_alloc(h, &h->coef, 6 * (size_t)h->plane * elem_r(h));
+  if (h->filtered) ok = ok && dev_alloc(h, &h->filt, (size_t)h->plane * elem_r(h));
   ok = ok && dev_alloc(h, &h->twx, (size_t)h->nx * elem_c(h));
   if (h->dim >= 2) ok = ok && dev_alloc(h, &h->twy, (size_t)h->ny * elem_c(h));
   if (h->dim == 3) ok = ok && dev_alloc(h, &h->twz, (size_t)h->nz * elem_c(h));
@@ -1060,6 +1091,48 @@ int ptf_set_flow_arrays(ptf_handle* h, const double* u, const double* v, const d
                            : phys_in<double>(h, src[q], where, (double*)dst[q], h->nphys, sc);
     if (rc) return rc;
   }
+  h->flow_layers = false;
+  h->have_flow = true;
+  return PTF_OK;
+}
+
+int ptf_set_flow_layers(ptf_handle* h, const double* u, const double* v, const double* U, int32_t where) {
+  if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
+  if (h->dim != 2) return fail(h, PTF_ERR_UNSUPPORTED, "layered flows are 2D (MultiLayerQG)");
+  if (!u || !v) return fail(h, PTF_ERR_ARG, "u and v are required");
+  if (check_where(h, where)) return PTF_ERR_ARG;
+  const long long B = h->cfg.batch, n = h->nphys * B;
+  if (!h->ul) {
+    const size_t bytes = (size_t)n * elem_r(h);
+    if (!dev_alloc(h, &h->ul, bytes) || !dev_alloc(h, &h->vl, bytes) ||
+        !dev_alloc(h, (void**)&h->layerU, (size_t)B * sizeof(double)))
+      return fail(h, PTF_ERR_MEMORY, "device allocation failed (layer flows)");
+  }
+  std::vector<double> Uh((size_t)B, 0.0);
+  if (U) Uh.assign(U, U + B);
+  cudaError_t e = cudaMemcpyAsync(h->layerU, Uh.data(), (size_t)B * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+  if (e != cudaSuccess) return cuda_fail(h, e, "layer mean flows");
+  // the flow is pre-scaled by -1/(2 nx ny) like ptf_set_flow_arrays
+  const double sc = -1.0 / (2.0 * (double)h->nphys);
+  const double* src[2] = {u, v};
+  void* dst[2] = {h->ul, h->vl};
+  for (int q = 0; q < 2; ++q) {
+    const double* dsrc = src[q];
+    if (where == PTF_HOST) {
+      e = cudaMemcpyAsync(h->stage, src[q], (size_t)n * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+      if (e != cudaSuccess) return cuda_fail(h, e, "host to device copy");
+      dsrc = h->stage;
+    }
+    e = h->fp32 ? launch_layers_in<float>(dsrc, (float*)dst[q], h->nphys, (int)B, q == 0 ? h->layerU : nullptr, sc, h->stream)
+                : launch_layers_in<double>(dsrc, (double*)dst[q], h->nphys, (int)B, q == 0 ? h->layerU : nullptr, sc, h->stream);
+    h->launches++;
+    if (e != cudaSuccess) return cuda_fail(h, e, "convert");
+    if (where == PTF_HOST) {
+      e = cudaStreamSynchronize(h->stream);
+      if (e != cudaSuccess) return cuda_fail(h, e, "synchronize");
+    }
+  }
+  h->flow_layers = true;
   h->have_flow = true;
   return PTF_OK;
 }

@@ -44,6 +44,10 @@ cudaError_t launch_solve_sums(const Tin* x, long long n, int batch, double* part
 // k0[4b] = Re src[b * per_solve]; dst[b * per_solve] = (k0[4b], 0)
 cudaError_t launch_k0_from_spec(const double2* src, long long per_solve, int batch, double* k0, cudaStream_t st);
 cudaError_t launch_k0_to_spec(double2* dst, long long per_solve, int batch, const double* k0, cudaStream_t st);
+// per-solve flows: dst[b n + i] = (src[b n + i] + U[b]) * scale (U may be null)
+template <typename T>
+cudaError_t launch_layers_in(const double* src, T* dst, long long n, int batch, const double* U, double scale,
+                             cudaStream_t st);
 // dst = src + (k0[4b] - sums[b]) / n per solve b
 template <typename T>
 cudaError_t launch_real_out_shift(const T* src, double* dst, long long n, int batch, const double* k0,

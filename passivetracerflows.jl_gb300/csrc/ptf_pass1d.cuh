@@ -18,6 +18,7 @@ template <typename T> struct Line1DArgs {
   const T* u;  // flow on the grid, pre-scaled by -1/(2 nx), shared by the batch
   const T* Ltab;
   const T* coef;
+  const T* filt;  // filtered steppers: spectral filter (null: none)
   const C* tw;
   T dkx, dt;
   int pitch, rows;  // rows = solves (even: an odd batch carries one zero solve)
@@ -111,7 +112,7 @@ __global__ void __launch_bounds__(256) line1d_kernel(Line1DArgs<T> a) {
         continue;
       }
       x = stage_combine<T, MODE>(o[j], k, a.s + r, a.si + r, a.acc + r, a.coef, (size_t)pitch, a.dt, true,
-                                 [&]() { return a.Ltab[k]; });
+                                 [&]() { return a.Ltab[k]; }, a.filt);
       if (a.k0 != nullptr && k == 0) {
         double* q = a.k0 + (size_t)(y0 + j) * 4;
         const double xd = k0_combine<MODE>(q, a.k0c, a.dt64, (double)o[j].x);

@@ -61,6 +61,7 @@ template <typename T> struct ColArgs {
   C* s;            // state (sol); COL_YINV3: the z-inverse Z1
   C* si;           // RK4: current stage input; ETDRK4: d = E2 a - zeta N(sol)
   C* acc;          // accumulator of the update
+  const T* filt;   // filtered steppers: the spectral filter the new state is multiplied by (null: none)
   C* A;            // F^-1(s_next)
   C* B;            // F^-1(i k s_next)
   C* Cout;         // COL_YINV3: F^-1(z2in)
@@ -198,7 +199,8 @@ __device__ __forceinline__ double column0_sum(const C* v, int w, int t, C* line0
 template <typename T, int MODE, typename C, typename LF>
 __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S, C* __restrict__ SI,
                                            C* __restrict__ AC, const T* __restrict__ cf,
-                                           size_t plane, T dt, bool store, LF&& Lf) {
+                                           size_t plane, T dt, bool store, LF&& Lf,
+                                           const T* __restrict__ filt = nullptr) {
   C x;
   if (MODE == COL_RK4_1) {
     const T L = Lf();
@@ -221,6 +223,7 @@ __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S,
     const C si = SI[o], ac = AC[o];
     C k; k.x = L * si.x + Nh.x; k.y = L * si.y + Nh.y;
     x.x = ac.x + (dt / 6) * k.x; x.y = ac.y + (dt / 6) * k.y;
+    if (filt) { const T f = filt[o]; x.x *= f; x.y *= f; }
     if (store) S[o] = x;
   } else if (MODE == COL_ETD_1) {
     // a = E2 s + zeta N(s) is the next input; stage 3's
@@ -251,6 +254,7 @@ __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S,
     const T ga = cf[o + 5 * plane];
     const C ac = AC[o];
     x.x = ac.x + ga * Nh.x; x.y = ac.y + ga * Nh.y;
+    if (filt) { const T f = filt[o]; x.x *= f; x.y *= f; }
     S[o] = x;
   }
   return x;
@@ -385,7 +389,8 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
       } else if (MODE == COL_FWD_N) {
         x = Nh; if (store) a.nout[boff + o] = Nh;
       } else {
-        x = stage_combine<T, MODE>(Nh, o, S, SI, AC, cf, plane, dt, store, [&]() { return Lval(Lt, o, i); });
+        x = stage_combine<T, MODE>(Nh, o, S, SI, AC, cf, plane, dt, store, [&]() { return Lval(Lt, o, i); },
+                                   (!BATCHED && a.filt) ? a.filt + toff : nullptr);
       }
       if (k0thr && i == 0) {
         // the (0,0) mode in FP64: {s, stage input (ETDRK4: d), acc, -} of this solve

@@ -164,6 +164,25 @@ cudaError_t launch_real_out_shift(const T* src, double* dst, long long n, int ba
   return cudaGetLastError();
 }
 
+// dst[b n + i] = (src[b n + i] + (U ? U[b] : 0)) * scale: per-solve flows
+template <typename T>
+__global__ void layers_in_kernel(const double* __restrict__ src, T* __restrict__ dst, long long n,
+                                 const double* __restrict__ U, double scale) {
+  const long long b = blockIdx.y;
+  const double off = U ? U[b] : 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[b * n + i] = (T)((src[b * n + i] + off) * scale);
+}
+template <typename T>
+cudaError_t launch_layers_in(const double* src, T* dst, long long n, int batch, const double* U, double scale,
+                             cudaStream_t st) {
+  const int gx = (grid_for(n * batch) + batch - 1) / batch;
+  layers_in_kernel<T><<<dim3(gx < 1 ? 1 : gx, batch), 256, 0, st>>>(src, dst, n, U, scale);
+  return cudaGetLastError();
+}
+template cudaError_t launch_layers_in<float>(const double*, float*, long long, int, const double*, double, cudaStream_t);
+template cudaError_t launch_layers_in<double>(const double*, double*, long long, int, const double*, double, cudaStream_t);
+
 template cudaError_t launch_solve_sums<double>(const double*, long long, int, double*, double*, int, cudaStream_t);
 template cudaError_t launch_solve_sums<float>(const float*, long long, int, double*, double*, int, cudaStream_t);
 template cudaError_t launch_real_out_shift<float>(const float*, double*, long long, int, const double*, const double*,

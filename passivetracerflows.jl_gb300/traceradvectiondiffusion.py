@@ -33,6 +33,7 @@ from . import _lib as L
 __all__ = [
     "CPU", "GPU", "noflow", "OneDAdvectingFlow", "TwoDAdvectingFlow", "ThreeDAdvectingFlow",
     "OneDGrid", "TwoDGrid", "ThreeDGrid", "gridpoints", "Problem", "set_c", "updatevars", "stepforward",
+    "MultiLayerQGFlow", "MultiLayerTracerProblem",
 ]
 
 
@@ -218,6 +219,13 @@ class Problem:
     stage combinations and the mean reported by ``vars.c`` -- in FP64.
     """
 
+    def __new__(cls, dev=None, *args, **kwargs):
+        # Problem(MQGprob; ...) (:225-250): a MultiLayerQG problem instead of a
+        # device and an advecting flow
+        if cls is Problem and _is_multilayer_flow(dev):
+            return object.__new__(MultiLayerTracerProblem)
+        return object.__new__(cls)
+
     def __init__(self, dev, advecting_flow: AdvectingFlow, **kwargs):
         if isinstance(dev, CPU) or dev is CPU:
             raise NotImplementedError("this package runs on the GPU only: pass GPU()")
@@ -244,9 +252,10 @@ class Problem:
         k0_fp64 = bool(kwargs.pop("k0_fp64", True))
         if kwargs:
             raise TypeError(f"unexpected keyword arguments: {sorted(kwargs)}")
-        steppers = {"RK4": L.PTF_RK4, "ETDRK4": L.PTF_ETDRK4}
+        steppers = {"RK4": L.PTF_RK4, "ETDRK4": L.PTF_ETDRK4, "FilteredRK4": L.PTF_FILTERED_RK4,
+                    "FilteredETDRK4": L.PTF_FILTERED_ETDRK4}
         if stepper not in steppers:
-            raise ValueError(f"stepper {stepper!r} is not supported (RK4, ETDRK4)")
+            raise ValueError(f"stepper {stepper!r} is not supported (RK4, ETDRK4, FilteredRK4, FilteredETDRK4)")
         if T in (np.float64, float, "Float64"):
             prec = L.PTF_FP64
         elif T in (np.float32, "Float32"):
@@ -438,3 +447,100 @@ def stepforward(prob: Problem, nsteps: int = 1):
     for _ in range(nsteps):
         prob._refresh_flow()
         L.check(lib.ptf_step(prob._h, 1), prob._h)
+
+
+# ---------------------------------------------------------------------------
+# MultiLayerQG-coupled tracer (src/traceradvectiondiffusion.jl:225-250,
+# :455-500, :556-566, :788-804)
+# ---------------------------------------------------------------------------
+def _is_multilayer_flow(obj):
+    return obj is not None and hasattr(obj, "vars") and hasattr(obj, "params") and \
+        hasattr(obj.params, "nlayers") and hasattr(obj, "grid") and hasattr(obj, "clock")
+
+
+class MultiLayerQGFlow:
+    """What the tracer needs of a ``GeophysicalFlows.MultiLayerQG`` problem:
+    ``grid`` (nx, Lx, ny, Ly), ``params.nlayers``, ``params.U`` (each layer's
+    imposed mean flow), ``clock.dt`` and ``vars.u``, ``vars.v`` (layer
+    velocities, ``(nlayers, ny, nx)``, NumPy or contiguous CUDA float64
+    tensors).  The QG model itself is not part of this package: the caller
+    advances it and updates ``vars``; ``step_until`` (optional) is called for
+    ``tracer_release_time > 0``."""
+
+    class _Params:
+        def __init__(self, nlayers, U):
+            self.nlayers = int(nlayers)
+            self.U = np.zeros(self.nlayers) if U is None else np.asarray(U, dtype=np.float64).reshape(self.nlayers)
+
+    class _Vars:
+        def __init__(self, u, v):
+            self.u, self.v = u, v
+
+    class _Clock:
+        def __init__(self, dt):
+            self.dt, self.t, self.step = float(dt), 0.0, 0
+
+    def __init__(self, *, nx, Lx=2 * math.pi, ny=None, Ly=None, nlayers, dt, U=None, u=None, v=None,
+                 step_until=None):
+        self.grid = _Grid(2, nx, Lx, ny, Ly)
+        self.params = self._Params(nlayers, U)
+        shape = (self.params.nlayers,) + self.grid.shape
+        self.vars = self._Vars(np.zeros(shape) if u is None else u, np.zeros(shape) if v is None else v)
+        self.clock = self._Clock(dt)
+        self._step_until = step_until
+
+    def step_until(self, t):
+        if self._step_until is None:
+            raise NotImplementedError("this MultiLayerQG stand-in cannot advance itself: pass step_until")
+        self._step_until(self, t)
+
+
+class MultiLayerTracerProblem(Problem):
+    """``TracerAdvectionDiffusion.Problem(MQGprob; κ=0.1, η=κ, stepper="FilteredRK4",
+    tracer_release_time=0)`` (``:225-250``): one tracer per layer, advected by
+    that layer's velocity plus its mean flow ``U`` (``calcN!``, ``:788-804``),
+    with ``L = -κ kr² - η l²`` (``:556-566``) and the MultiLayerQG problem's
+    grid and ``dt``.  The layers are the solves of one batched handle; the
+    layer velocities are read from ``MQGprob.vars`` before every step, as
+    ``calcN!`` reads them.  Extension: ``T=np.float32``."""
+
+    def __init__(self, MQGprob, κ=0.1, η=None, stepper="FilteredRK4", tracer_release_time=0, T=np.float64, **kw):
+        κ = float(kw.pop("kappa", κ))
+        η = κ if η is None else float(η)
+        η = float(kw.pop("eta", η))
+        if kw:
+            raise TypeError(f"unexpected keyword arguments: {sorted(kw)}")
+        if tracer_release_time < 0:
+            raise ValueError("tracer_release_time must be non-negative!")
+        if tracer_release_time > 0:
+            MQGprob.step_until(tracer_release_time)
+        self.MQGprob = MQGprob
+        g = MQGprob.grid
+        nl = int(MQGprob.params.nlayers)
+        flow = AdvectingFlow(steadyflow=False, dim=2)
+        super().__init__(GPU(), flow, nx=g.nx, Lx=g.Lx, ny=g.ny, Ly=g.Ly, κ=κ, η=η, dt=MQGprob.clock.dt,
+                         stepper=stepper, T=T, batch=nl)
+        self.nlayers = nl
+        self.tracer_release_time = float(tracer_release_time)
+        if nl == 1:
+            self.vars = Vars(np.zeros((1,) + self.grid.shape))
+        self._refresh_flow()
+
+    def _refresh_flow(self):
+        """``u = MQGprob.vars.u + MQGprob.params.U``, ``v = MQGprob.vars.v`` (``:794-795``)."""
+        mq = self.MQGprob
+        U = np.asarray(getattr(mq.params, "U", np.zeros(self.nlayers)), dtype=np.float64).reshape(self.nlayers)
+        shape = (self.nlayers,) + self.grid.shape
+        ptrs, keep, where = [], [], L.PTF_HOST
+        for a in (mq.vars.u, mq.vars.v):
+            if hasattr(a, "is_cuda") and a.is_cuda:
+                where = L.PTF_DEVICE
+                ptrs.append(ct.c_void_p(a.data_ptr()))
+                keep.append(a)
+            else:
+                a = np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64), shape))
+                keep.append(a)
+                ptrs.append(a.ctypes.data_as(ct.c_void_p))
+        Uc = np.ascontiguousarray(U)
+        L.check(L.load().ptf_set_flow_layers(self._h, ptrs[0], ptrs[1], Uc.ctypes.data_as(ct.c_void_p), where),
+                self._h)

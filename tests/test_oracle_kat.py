@@ -84,3 +84,28 @@ def test_etdrk4_coefficients_limits(oracle):
     zz = -50.0 * dt
     assert abs(z[2] - dt * (np.exp(zz / 2) - 1) / zz) < 1e-15
     assert abs(a[2] - dt * (-4 - zz + np.exp(zz) * (4 - 3 * zz + zz * zz)) / zz ** 3) < 1e-12
+
+
+def test_filter_shape(oracle):
+    """FourierFlows' filter: 1 below innerK = 0.65, tol = 1e-15 at K = outerK = 1
+    (the Nyquist wavenumber of a 1D grid), monotone in between."""
+    g = oracle.Grid(1, 64, 2 * np.pi)
+    f = oracle.makefilter(g)
+    K = g.kr * g.dx / np.pi
+    assert np.all(f[K < 0.65] == 1.0)
+    assert abs(f[-1] - 1e-15) < 1e-17
+    assert np.all(np.diff(f) <= 0)
+
+
+def test_filtered_step_is_step_then_filter(oracle):
+    r = oracle.Problem(oracle.TwoDAdvectingFlow(u=lambda x, y: np.sin(y), v=lambda x, y: 0 * x), nx=32,
+                       kappa=1e-3, dt=0.01, stepper="RK4")
+    q = oracle.Problem(oracle.TwoDAdvectingFlow(u=lambda x, y: np.sin(y), v=lambda x, y: 0 * x), nx=32,
+                       kappa=1e-3, dt=0.01, stepper="FilteredRK4")
+    x, y = r.grid.gridpoints()
+    c0 = np.exp(-(x ** 2 + y ** 2))
+    oracle.set_c(r, c0)
+    oracle.set_c(q, c0)
+    oracle.stepforward(r, 1)
+    oracle.stepforward(q, 1)
+    assert np.allclose(q.sol, r.sol * oracle.makefilter(r.grid), rtol=0, atol=1e-14)
