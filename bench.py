@@ -494,12 +494,12 @@ def run_ours(args):
     # ---------------- other configurations (rank 0, bounded) ----------------
     configs = {}
     if rank == 0 and not args.only_main:
-        for key, fn in (("3d_abc_256", lambda: run_config3(pkg, torch)),
-                        ("ensemble_256_solves", lambda: run_config4(pkg, torch, args.ensemble_steps)),
+        for key, fn in (("3d_abc_256", lambda: run_abc3d_256(pkg, torch)),
+                        ("ensemble_256_solves", lambda: run_ensemble_256(pkg, torch, args.ensemble_steps)),
                         ("ensemble_256_solves_clock_t",
-                         lambda: run_config4(pkg, torch, args.ensemble_steps, time_mode="clock")),
-                        ("served_fp32", lambda: run_config5(pkg, np.float32, args.serve_requests, args.serve_rate)),
-                        ("served_fp64", lambda: run_config5(pkg, np.float64, args.serve_requests_fp64,
+                         lambda: run_ensemble_256(pkg, torch, args.ensemble_steps, time_mode="clock")),
+                        ("served_fp32", lambda: run_served_stream(pkg, np.float32, args.serve_requests, args.serve_rate)),
+                        ("served_fp64", lambda: run_served_stream(pkg, np.float64, args.serve_requests_fp64,
                                                             args.serve_rate / 4))):
             try:
                 configs[key] = fn()
@@ -564,7 +564,7 @@ def run_ours(args):
 # ---------------------------------------------------------------------------
 # Secondary configurations (bounded samples; reported inside the one JSON line)
 # ---------------------------------------------------------------------------
-def run_config3(pkg, torch, steps=10):
+def run_abc3d_256(pkg, torch, steps=10):
     """3D ABC flow, 256³, ETDRK4, κ=η=ι=5e-4, dt=0.005, Gaussian σ=0.3 at the
     centre: FP32 and FP64 single solves; FP32 compared with the FP64 GPU solve."""
     n, dt = 256, 0.005
@@ -601,7 +601,7 @@ def run_config3(pkg, torch, steps=10):
     return out
 
 
-def run_config4(pkg, torch, steps, seed=2024, time_mode="stage"):
+def run_ensemble_256(pkg, torch, steps, seed=2024, time_mode="stage"):
     """Batched ensemble: 256 2D solves, n uniform in {64,128,256,512}, κ
     log-uniform in [1e-4,1e-2], ψ = cos(x + 0.3 sin t) cos y re-evaluated at
     every RK4 stage (time_mode "stage") or frozen at clock.t for the step as
@@ -700,7 +700,7 @@ def random_phase_flow(n, rng, dim=2, kmin=4, kmax=16, L=2 * np.pi):
     return u / rms, v / rms, w / rms
 
 
-def run_config5(pkg, T, nreq, rate, seed=5150):
+def run_served_stream(pkg, T, nreq, rate, seed=5150):
     """Served stream: requests with Poisson arrivals; each a 2D grid from
     {64²..1024²} or 3D 128³ (one in ten), steps log-uniform in [100,5000], κ
     log-uniform in [1e-4,1e-2], random-phase flow; dt per request for an

@@ -161,8 +161,8 @@ def test_errors_are_raised_not_faults(gpu):
         gpu.stepforward(p, -1)
 
 
-def test_golden_config1_full(gpu, oracle):
-    """BASELINE config 1 (128² cellular flow, RK4, dt=0.01, 2000 steps, FP64) vs the
+def test_golden_cellular128_rk4_2000_steps(gpu, oracle):
+    """The 128² cellular-flow workload (RK4, dt=0.01, 2000 steps, FP64) vs the
     golden fixture: the reference target is <= 1e-10."""
     from pathlib import Path
     g = np.load(Path(__file__).resolve().parent / "golden" / "cellular128_rk4.npz")
