@@ -212,6 +212,9 @@ typedef struct ptf_batch_config {
   int32_t slots_per_bucket; /* solves per same-size bucket (0: about 1 GB of fields per bucket) */
   int32_t use_graph;        /* replay steps from a captured CUDA graph */
   int32_t max_slots;        /* total slots over all buckets */
+  int32_t persistent;       /* 1: one persistent kernel per stage (items from an atomic counter, a
+                               bounded wait between a bucket's row and column items); 0 (default):
+                               a row launch and a column launch per stage, one block per item */
 } ptf_batch_config;
 
 typedef struct ptf_batch ptf_batch;

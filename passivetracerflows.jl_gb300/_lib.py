@@ -47,7 +47,7 @@ class PtfSolveDesc(ct.Structure):
 
 class PtfBatchConfig(ct.Structure):
     _fields_ = [("precision", ct.c_int32), ("memory_budget", ct.c_int64), ("slots_per_bucket", ct.c_int32),
-                ("use_graph", ct.c_int32), ("max_slots", ct.c_int32)]
+                ("use_graph", ct.c_int32), ("max_slots", ct.c_int32), ("persistent", ct.c_int32)]
 
 
 class PtfServerConfig(ct.Structure):

@@ -72,10 +72,12 @@ _PREC = {np.float64: L.PTF_FP64, np.float32: L.PTF_FP32}
 
 
 class BatchedProblem:
-    """Independent 2D solves stepped together (RK4; one persistent kernel per
-    stage for all solves, steps replayed from a captured CUDA graph)."""
+    """Independent 2D solves stepped together (RK4; per stage one row launch and
+    one column launch over all solves' work items -- or one persistent kernel
+    with ``persistent=True`` -- steps replayed from a captured CUDA graph)."""
 
-    def __init__(self, T=np.float32, memory_budget=0, slots_per_bucket=0, use_graph=True, max_slots=4096):
+    def __init__(self, T=np.float32, memory_budget=0, slots_per_bucket=0, use_graph=True, max_slots=4096,
+                 persistent=False):
         lib = L.load()
         cfg = L.PtfBatchConfig()
         lib.ptf_batch_config_default(ct.byref(cfg))
@@ -84,6 +86,7 @@ class BatchedProblem:
         cfg.slots_per_bucket = int(slots_per_bucket)
         cfg.use_graph = 1 if use_graph else 0
         cfg.max_slots = int(max_slots)
+        cfg.persistent = 1 if persistent else 0
         h = ct.c_void_p()
         L.check(lib.ptf_batch_create(ct.byref(cfg), ct.byref(h)), None)
         self._h = h

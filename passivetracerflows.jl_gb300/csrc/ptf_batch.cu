@@ -49,6 +49,15 @@ template <typename T> __global__ void batch_clock_kernel(SlotParams<T>* slots, i
   extern template cudaError_t launch_batch_stage<T, M>(const BatchPlan<T>*, unsigned int*, int*, T, int, size_t, \
                                                        cudaStream_t);                                          \
   extern template cudaError_t setup_batch_stage<T, M>(size_t, int*);
+#define PTF_EXTERN_ITEMS(T, M)                                                                           \
+  extern template cudaError_t launch_batch_cols<T, M>(const BatchPlan<T>*, int, size_t, cudaStream_t); \
+  extern template cudaError_t setup_batch_items<T, M>(size_t);
+PTF_EXTERN_ITEMS(float, COL_RK4_1) PTF_EXTERN_ITEMS(float, COL_RK4_2) PTF_EXTERN_ITEMS(float, COL_RK4_3)
+PTF_EXTERN_ITEMS(float, COL_RK4_4) PTF_EXTERN_ITEMS(double, COL_RK4_1) PTF_EXTERN_ITEMS(double, COL_RK4_2)
+PTF_EXTERN_ITEMS(double, COL_RK4_3) PTF_EXTERN_ITEMS(double, COL_RK4_4)
+#undef PTF_EXTERN_ITEMS
+extern template cudaError_t launch_batch_rows<float>(const BatchPlan<float>*, float, int, size_t, cudaStream_t);
+extern template cudaError_t launch_batch_rows<double>(const BatchPlan<double>*, double, int, size_t, cudaStream_t);
 PTF_EXTERN_STAGE(float, COL_RK4_1) PTF_EXTERN_STAGE(float, COL_RK4_2) PTF_EXTERN_STAGE(float, COL_RK4_3)
 PTF_EXTERN_STAGE(float, COL_RK4_4) PTF_EXTERN_STAGE(double, COL_RK4_1) PTF_EXTERN_STAGE(double, COL_RK4_2)
 PTF_EXTERN_STAGE(double, COL_RK4_3) PTF_EXTERN_STAGE(double, COL_RK4_4)
@@ -96,7 +105,7 @@ struct ptf_batch {
   std::map<long long, SolveRef> solves;
   long long next_id = 1;
   bool plan_dirty = true;
-  int plan_total = 0;
+  int plan_total = 0, plan_row_total = 0;
   std::vector<int> plan_lists;      // active slots per bucket of the current plan
   std::vector<int> plan_buckets;
   int grid = 0;
@@ -378,6 +387,7 @@ template <typename T> int build_plan(ptf_batch* b) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   if (e != cudaSuccess) return bcuda(b, e, "plan upload");
   b->plan_total = plan.total;
+  b->plan_row_total = plan.row_total;
   b->plan_dirty = false;
   if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
   if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
@@ -387,6 +397,23 @@ template <typename T> int build_plan(ptf_batch* b) {
 template <typename T> cudaError_t enqueue_step(ptf_batch* b) {
   const T cs[4] = {(T)0, (T)0.5, (T)0.5, (T)1};
   const BatchPlan<T>* plan = (const BatchPlan<T>*)b->plan_dev;
+  if (!b->cfg.persistent) {
+    const int rows = b->plan_row_total, cols = b->plan_total - b->plan_row_total;
+    for (int st = 0; st < 4; ++st) {
+      cudaError_t e = rows > 0 ? launch_batch_rows<T>(plan, cs[st], rows, b->smem, b->stream) : cudaSuccess;
+      if (e == cudaSuccess && cols > 0) {
+        switch (st) {
+          case 0: e = launch_batch_cols<T, COL_RK4_1>(plan, cols, b->smem, b->stream); break;
+          case 1: e = launch_batch_cols<T, COL_RK4_2>(plan, cols, b->smem, b->stream); break;
+          case 2: e = launch_batch_cols<T, COL_RK4_3>(plan, cols, b->smem, b->stream); break;
+          default: e = launch_batch_cols<T, COL_RK4_4>(plan, cols, b->smem, b->stream); break;
+        }
+      }
+      if (e != cudaSuccess) return e;
+    }
+    batch_clock_kernel<T><<<(b->slot_used + 255) / 256, 256, 0, b->stream>>>((SlotParams<T>*)b->slots_dev, b->slot_used);
+    return cudaGetLastError();
+  }
   for (int st = 0; st < 4; ++st) {
     cudaError_t e = cudaMemsetAsync(b->ctr, 0, (kMaxBuckets + 1) * sizeof(unsigned int), b->stream);
     if (e != cudaSuccess) return e;
@@ -416,6 +443,13 @@ template <typename T> int setup_kernels(ptf_batch* b) {
     }
     if (e != cudaSuccess) return bcuda(b, e, "batched kernel set-up");
     occ = std::min(occ, o);
+    switch (st) {
+      case 0: e = setup_batch_items<T, COL_RK4_1>(b->smem); break;
+      case 1: e = setup_batch_items<T, COL_RK4_2>(b->smem); break;
+      case 2: e = setup_batch_items<T, COL_RK4_3>(b->smem); break;
+      default: e = setup_batch_items<T, COL_RK4_4>(b->smem); break;
+    }
+    if (e != cudaSuccess) return bcuda(b, e, "batched kernel set-up");
   }
   if (occ < 1) return bfail(b, PTF_ERR_UNSUPPORTED, "batched kernel does not fit on an SM");
   int dev = 0, sms = 0;

@@ -111,6 +111,63 @@ batch_stage_kernel(const BatchPlan<T>* __restrict__ plan, unsigned int* ctr, int
   }
 }
 
+// ---------------------------------------------------------------------------
+// One block per work item instead: a row launch over every bucket's row
+// items, then a column launch over the column items; the hardware schedules
+// the blocks and the kernel boundary is the dependency.  Same items, same
+// bodies as the persistent kernel.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kBatchThreads, BatchBounds<T>::blocks)
+batch_row_kernel(const BatchPlan<T>* __restrict__ plan, T stage_c) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int item = blockIdx.x, nb = plan->nb;
+  int b = 0;
+  while (b + 1 < nb && item >= plan->b[b + 1].row_begin) ++b;
+  RowArgs<T> ra = plan->b[b].row;
+  ra.stage_c = stage_c;
+  const int local = item - plan->b[b].row_begin;
+  switch (plan->b[b].n) {
+#define PTF_CASE(n) case n: row_body<T, n, true>(ra, local, 0, smem); break;
+    PTF_BATCH_SIZES(PTF_CASE)
+#undef PTF_CASE
+    default: break;
+  }
+}
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kBatchThreads, BatchBounds<T>::blocks)
+batch_col_kernel(const BatchPlan<T>* __restrict__ plan) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int item = plan->row_total + blockIdx.x, nb = plan->nb;
+  int b = 0;
+  while (b + 1 < nb && item >= plan->b[b + 1].col_begin) ++b;
+  const ColArgs<T> ca = plan->b[b].col;
+  const int local = item - plan->b[b].col_begin;
+  switch (plan->b[b].n) {
+    // buckets hold square grids: the row pitch is square_pitch<n>()
+#define PTF_CASE(n) case n: col_body<T, n, MODE, true, square_pitch<n>()>(ca, local, 0, smem); break;
+    PTF_BATCH_SIZES(PTF_CASE)
+#undef PTF_CASE
+    default: break;
+  }
+}
+template <typename T>
+cudaError_t launch_batch_rows(const BatchPlan<T>* plan, T stage_c, int nitems, size_t smem, cudaStream_t st) {
+  batch_row_kernel<T><<<nitems, kBatchThreads, smem, st>>>(plan, stage_c);
+  return cudaGetLastError();
+}
+template <typename T, int MODE>
+cudaError_t launch_batch_cols(const BatchPlan<T>* plan, int nitems, size_t smem, cudaStream_t st) {
+  batch_col_kernel<T, MODE><<<nitems, kBatchThreads, smem, st>>>(plan);
+  return cudaGetLastError();
+}
+template <typename T, int MODE> cudaError_t setup_batch_items(size_t smem) {
+  cudaError_t e = cudaFuncSetAttribute(batch_col_kernel<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess && MODE == COL_RK4_1)
+    e = cudaFuncSetAttribute(batch_row_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return e;
+}
+
 // Launcher and set-up of one (precision, stage) kernel; instantiated in
 // ptf_batch_inst.cu objects.
 template <typename T, int MODE>
