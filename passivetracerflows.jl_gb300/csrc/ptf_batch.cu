@@ -2,18 +2,19 @@
 // together on one GPU.
 //
 // Solves of the same size share a bucket (fixed number of slots, one set of
-// fields per slot).  Each RK4 stage of every bucket is ONE launch of a
-// persistent kernel (batch_stage_kernel): blocks take work items from an
-// atomic counter -- first the row-pass tiles of every bucket, then the
-// column-pass tiles -- and a column tile of bucket b starts once all row
-// tiles of b are done (a per-bucket completion counter; the wait is bounded
-// and sets an error flag if it ever runs out).  Because items are handed out
-// in order, every row tile a column tile waits for is already running on a
-// resident block, so the wait always ends.  After the four stages a clock
+// fields per slot).  The work of an RK4 stage over every bucket is a list of
+// items -- the row-pass tiles of every bucket, then the column-pass tiles.
+// By default a stage is a row launch and a column launch, one block per
+// item.  With cfg.persistent it is ONE launch of a persistent kernel
+// (batch_stage_kernel): blocks take items from an atomic counter and a
+// column tile of bucket b starts once all row tiles of b are done (a
+// per-bucket completion counter; the wait is bounded and sets an error flag
+// if it ever runs out; items are handed out in order, so every row tile a
+// column tile waits for is already running on a resident block, and the
+// wait always ends).  After the four stages a clock
 // kernel advances each active solve's t and step and retires solves that
 // reached their own step count (their fields are no longer written).  One
-// step -- four counter resets, four stage launches, the clock kernel -- is
-// captured once in a CUDA graph and replayed.
+// step is captured once in a CUDA graph and replayed.
 //
 // Per-slot parameters give each solve its own kappa, dt, clock and flow: an
 // array (steady) or the analytic cellular flow re-evaluated at clock.t
@@ -485,7 +486,9 @@ template <typename T> int step_impl(ptf_batch* b, long long nsteps) {
       if (e != cudaSuccess) return bcuda(b, e, "step launch");
     }
   }
-  b->launches += 5 * nsteps;
+  // kernels per step: 4 stage launches (persistent) or up to 4 x (rows + columns), then the clock kernel
+  const long long per_step = b->cfg.persistent ? 5 : 4 * ((b->plan_row_total > 0) + (b->plan_total > b->plan_row_total)) + 1;
+  b->launches += per_step * nsteps;
   // solves that finished are retired from the plan at the next call
   b->plan_dirty = true;
   return PTF_OK;
