@@ -136,6 +136,9 @@ __device__ __forceinline__ T kval(int p, T dk) { return (T)(p < N / 2 ? p : p - 
 #ifndef PTF_COL_THREADS_F32
 #define PTF_COL_THREADS_F32 256
 #endif
+#ifndef PTF_EARLY_OPERAND
+#define PTF_EARLY_OPERAND 1  // fetch a stage operand ahead with cp.async (see col_body)
+#endif
 template <typename T> struct ColBounds { static constexpr int threads = 256, blocks = PTF_COL_MINB_F64; };
 template <> struct ColBounds<float> { static constexpr int threads = PTF_COL_THREADS_F32, blocks = PTF_COL_MINB_F32; };
 
@@ -196,23 +199,36 @@ __device__ __forceinline__ double column0_sum(const C* v, int w, int t, C* line0
 // the state arrays S (sol), SI (RK4 stage input / ETDRK4 d = E2 a - zeta N(sol)),
 // AC (accumulator).  RK4 stores only when `store` (batched slots); Lf() gives
 // the linear operator at o.
-template <typename T, int MODE, typename C, typename LF>
+// The operand of a stage combination the column pass fetches ahead into
+// shared memory (cp.async, before the forward transform): 1 = S, 2 = SI,
+// 3 = AC, 0 = none -- the first state operand each mode reads.
+__host__ __device__ constexpr int early_operand(int mode) {
+  return (mode == COL_RK4_1 || mode == COL_ETD_1 || mode == COL_ETD_2) ? 1
+         : (mode == COL_RK4_2 || mode == COL_RK4_3 || mode == COL_RK4_4 || mode == COL_ETD_3) ? 2
+         : (mode == COL_ETD_4) ? 3 : 0;
+}
+
+template <typename T, int MODE, int PF = 0, typename C, typename LF>
 __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S, C* __restrict__ SI,
                                            C* __restrict__ AC, const T* __restrict__ cf,
                                            size_t plane, T dt, bool store, LF&& Lf,
-                                           const T* __restrict__ filt = nullptr) {
+                                           const T* __restrict__ filt = nullptr, C pre = C()) {
+  // PF != 0: operand early_operand(MODE) was fetched ahead; its value is `pre`
+  auto ldS = [&]() { return PF == 1 ? pre : S[o]; };
+  auto ldSI = [&]() { return PF == 2 ? pre : SI[o]; };
+  auto ldAC = [&]() { return PF == 3 ? pre : AC[o]; };
   C x;
   if (MODE == COL_RK4_1) {
     const T L = Lf();
-    const C s = S[o];
+    const C s = ldS();
     C k; k.x = L * s.x + Nh.x; k.y = L * s.y + Nh.y;
     C ac; ac.x = s.x + (dt / 6) * k.x; ac.y = s.y + (dt / 6) * k.y;
     x.x = s.x + (dt / 2) * k.x; x.y = s.y + (dt / 2) * k.y;
     if (store) { AC[o] = ac; SI[o] = x; }
   } else if (MODE == COL_RK4_2 || MODE == COL_RK4_3) {
     const T L = Lf();
-    const C si = SI[o], s = S[o];
-    C ac = AC[o];
+    const C si = ldSI(), s = ldS();
+    C ac = ldAC();
     C k; k.x = L * si.x + Nh.x; k.y = L * si.y + Nh.y;
     ac.x += (dt / 3) * k.x; ac.y += (dt / 3) * k.y;
     const T h = (MODE == COL_RK4_2) ? dt / 2 : dt;
@@ -220,7 +236,7 @@ __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S,
     if (store) { AC[o] = ac; SI[o] = x; }
   } else if (MODE == COL_RK4_4) {
     const T L = Lf();
-    const C si = SI[o], ac = AC[o];
+    const C si = ldSI(), ac = ldAC();
     C k; k.x = L * si.x + Nh.x; k.y = L * si.y + Nh.y;
     x.x = ac.x + (dt / 6) * k.x; x.y = ac.y + (dt / 6) * k.y;
     if (filt) { const T f = filt[o]; x.x *= f; x.y *= f; }
@@ -230,7 +246,7 @@ __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S,
     // c = E2 a + zeta (2 N(b) - N(s)) = d + 2 zeta N(b) needs only
     // d = E2 a - zeta N(s), stored in SI in place of a and N(s)
     const T Ee = cf[o], E2 = cf[o + plane], ze = cf[o + 2 * plane], al = cf[o + 3 * plane];
-    const C s = S[o];
+    const C s = ldS();
     C ac; ac.x = Ee * s.x + al * Nh.x; ac.y = Ee * s.y + al * Nh.y;
     AC[o] = ac;
     x.x = E2 * s.x + ze * Nh.x; x.y = E2 * s.y + ze * Nh.y;
@@ -238,21 +254,21 @@ __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S,
     SI[o] = d;
   } else if (MODE == COL_ETD_2) {
     const T E2 = cf[o + plane], ze = cf[o + 2 * plane], be = cf[o + 4 * plane];
-    const C s = S[o];
-    C ac = AC[o];
+    const C s = ldS();
+    C ac = ldAC();
     ac.x += 2 * be * Nh.x; ac.y += 2 * be * Nh.y;
     AC[o] = ac;
     x.x = E2 * s.x + ze * Nh.x; x.y = E2 * s.y + ze * Nh.y;
   } else if (MODE == COL_ETD_3) {
     const T ze = cf[o + 2 * plane], be = cf[o + 4 * plane];
-    const C d = SI[o];
-    C ac = AC[o];
+    const C d = ldSI();
+    C ac = ldAC();
     ac.x += 2 * be * Nh.x; ac.y += 2 * be * Nh.y;
     AC[o] = ac;
     x.x = d.x + 2 * ze * Nh.x; x.y = d.y + 2 * ze * Nh.y;
   } else {  // COL_ETD_4
     const T ga = cf[o + 5 * plane];
-    const C ac = AC[o];
+    const C ac = ldAC();
     x.x = ac.x + ga * Nh.x; x.y = ac.y + ga * Nh.y;
     if (filt) { const T f = filt[o]; x.x *= f; x.y *= f; }
     S[o] = x;
@@ -339,6 +355,16 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
   constexpr bool K0MODE = (MODE >= COL_RK4_1 && MODE <= COL_ETD_4) || MODE == COL_FWD_STORE;
   const bool k0blk = !BATCHED && K0MODE && a.k0 != nullptr && tile == 0;  // uniform across the block
   double k0N = 0;
+  // the combination's first state operand, fetched into this thread's park
+  // slots while the forward transform runs (the slots are free until the
+  // combination writes the next stage input there)
+  constexpr int PF = (PTF_EARLY_OPERAND && !BATCHED) ? early_operand(MODE) : 0;
+  if (PF) {
+    const C* __restrict__ op = (PF == 1 ? a.s : PF == 2 ? a.si : a.acc) + boff;
+#pragma unroll
+    for (int i = 0; i < E; ++i) cp_async<sizeof(C)>(park + i * nthr + threadIdx.x, op + PTF_OFF(RF, i));
+    cp_async_commit();
+  }
   C v[E];
   if (MODE != COL_PROLOGUE && MODE != COL_YINV3) {
     const C* __restrict__ src = a.nxin + boff;
@@ -389,8 +415,11 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
       } else if (MODE == COL_FWD_N) {
         x = Nh; if (store) a.nout[boff + o] = Nh;
       } else {
-        x = stage_combine<T, MODE>(Nh, o, S, SI, AC, cf, plane, dt, store, [&]() { return Lval(Lt, o, i); },
-                                   (!BATCHED && a.filt) ? a.filt + toff : nullptr);
+        if (PF && i == 0) cp_async_wait_all();
+        auto lf = [&]() { return Lval(Lt, o, i); };
+        x = stage_combine<T, MODE, PF>(Nh, o, S, SI, AC, cf, plane, dt, store, lf,
+                                                        (!BATCHED && a.filt) ? a.filt + toff : nullptr,
+                                                        PF ? park[i * nthr + threadIdx.x] : C());
       }
       if (k0thr && i == 0) {
         // the (0,0) mode in FP64: {s, stage input (ETDRK4: d), acc, -} of this solve
