@@ -133,13 +133,13 @@ def test_persistent_and_item_launches_agree(gpu, oracle, T, tol):
     """The persistent kernel and the two launches per stage run the same item
     bodies: same results for a mixed-size batch with its own step counts."""
     rng = np.random.default_rng(11)
+    cases = [(n, steps, gauss(n, *rng.uniform(-2, 2, 2), 0.3)) for n, steps in ((64, 7), (128, 12), (64, 12), (256, 5))]
     out = []
     for persistent in (False, True):
         b = gpu.BatchedProblem(T=T, slots_per_bucket=3, persistent=persistent)
         ids = []
-        for n, steps in ((64, 7), (128, 12), (64, 12), (256, 5)):
+        for n, steps, c0 in cases:
             u, v = cellular_arrays(n, k=2)
-            c0 = gauss(n, *rng.uniform(-2, 2, 2), 0.3)
             ids.append(b.add(gpu.SolveSpec(n=n, nsteps=steps, dt=0.004, kappa=2e-3, flow="arrays"), c0, u, v))
         b.step(12)
         out.append([b.get_c(i) for i in ids])
