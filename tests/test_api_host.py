@@ -46,3 +46,41 @@ def test_grid_matches_oracle(pkg, oracle):
     X, Y = pkg.gridpoints(g)
     Xo, Yo = o.gridpoints()
     assert np.array_equal(X, Xo) and np.array_equal(Y, Yo)
+
+
+def test_one_d_grid_and_gridpoints(pkg, oracle):
+    g = pkg.OneDGrid(nx=64, Lx=3.0)
+    x = pkg.gridpoints(g)
+    assert x.shape == (64,) and g.spec_shape == (33,)
+    r = oracle.Grid(1, 64, 3.0)
+    assert np.array_equal(x, r.gridpoints()[0])
+    assert np.allclose(g.Krsq, r.Krsq)
+
+
+def test_filtered_steppers_are_accepted_names(pkg):
+    """FilteredRK4 / FilteredETDRK4 pass the host checks (the handle itself
+    needs a GPU: without one the call gets as far as the device)."""
+    from ptf_gb300._lib import PtfArgumentError
+    for st in ("FilteredRK4", "FilteredETDRK4"):
+        with pytest.raises(Exception) as e:
+            pkg.Problem(pkg.GPU(), pkg.TwoDAdvectingFlow(), nx=32, stepper=st)
+        assert not isinstance(e.value, (ValueError, PtfArgumentError))
+
+
+def test_multilayer_dispatch_and_arguments(pkg):
+    """Problem(MQGprob; ...) dispatches on a MultiLayerQG-like first argument
+    (:225-250) and checks tracer_release_time before touching the device."""
+    mq = pkg.MultiLayerQGFlow(nx=32, nlayers=3, dt=0.01, U=[0.1, 0.0, -0.1])
+    assert mq.params.nlayers == 3 and mq.vars.u.shape == (3, 32, 32) and mq.clock.dt == 0.01
+    assert np.allclose(mq.params.U, [0.1, 0.0, -0.1])
+    with pytest.raises(ValueError):
+        pkg.Problem(mq, tracer_release_time=-1.0)
+    with pytest.raises(NotImplementedError):
+        pkg.Problem(mq, tracer_release_time=0.5)  # the stand-in cannot advance itself
+    with pytest.raises(TypeError):
+        pkg.Problem(mq, nsteps=3)
+    seen = []
+    mq2 = pkg.MultiLayerQGFlow(nx=32, nlayers=2, dt=0.01, step_until=lambda m, t: seen.append(t))
+    with pytest.raises(Exception):  # no GPU here: fails at the device, after stepping the flow
+        pkg.Problem(mq2, tracer_release_time=0.25)
+    assert seen == [0.25]
