@@ -94,6 +94,23 @@ const char* ptf_last_error(const ptf_handle* h);
  * ConstDiffSteadyFlowParams (:436-452).  Also used for a time-varying flow
  * re-evaluated by the caller at clock.t before each step (:715-718). */
 int ptf_set_flow_arrays(ptf_handle* h, const double* u, const double* v, const double* w, int32_t where);
+/* A flow given by formula and evaluated on the device: PTF_FLOW_CELLULAR
+ * (2D; Kx, Ky integer wavenumbers in units of 2 pi / L; time-dependent when
+ * eps and omega are non-zero) or PTF_FLOW_ABC (3D; A, B, C).  A
+ * time-dependent flow is re-evaluated at clock.t before every step, inside
+ * ptf_step, as the reference's time-varying calcN! evaluates it at clock.t
+ * for all four stages (:715-718) -- without a host evaluation or a copy per
+ * step.  No reference counterpart as an entry point: the reference takes
+ * flows as Julia functions; this covers the analytic flows of its examples
+ * and tests.  ptf_set_flow_arrays / ptf_set_flow_layers replace it. */
+typedef struct ptf_flow_desc {
+  int32_t kind;        /* PTF_FLOW_CELLULAR or PTF_FLOW_ABC */
+  double U, eps, omega;
+  int32_t Kx, Ky;
+  double A, B, C;
+} ptf_flow_desc;
+int ptf_set_flow_analytic(ptf_handle* h, const ptf_flow_desc* d);
+
 /* One flow per solve of a 2D batch -- the layers of the MultiLayerQG-coupled
  * tracer (Problem(MQGprob), :225-250; calcN!, :788-804): solve j is advected
  * by u_j + U[j], v_j, with u, v holding batch*nx*ny values (layer-major) and
@@ -187,8 +204,10 @@ int32_t ptf_abi_version(void);
  * ------------------------------------------------------------------------- */
 enum ptf_flow_kind {
   PTF_FLOW_ARRAYS = 0,   /* steady flow given as grid arrays u, v */
-  PTF_FLOW_CELLULAR = 1  /* psi = U cos(Kx x + eps sin(omega t)) cos(Ky y), u = -dpsi/dy, v = dpsi/dx,
+  PTF_FLOW_CELLULAR = 1, /* psi = U cos(Kx x + eps sin(omega t)) cos(Ky y), u = -dpsi/dy, v = dpsi/dx,
                             evaluated on the device at clock.t (PTF_CLOCK_T) or at stage times */
+  PTF_FLOW_ABC = 2       /* 3D handles only: u = A sin z + C cos y, v = B sin x + A cos z,
+                            w = C sin y + B cos x (steady) */
 };
 
 typedef struct ptf_solve_desc {

@@ -30,7 +30,12 @@ class PtfConfig(ct.Structure):
     ]
 
 
-PTF_FLOW_ARRAYS, PTF_FLOW_CELLULAR = 0, 1
+PTF_FLOW_ARRAYS, PTF_FLOW_CELLULAR, PTF_FLOW_ABC = 0, 1, 2
+
+
+class PtfFlowDesc(ct.Structure):
+    _fields_ = [("kind", ct.c_int32), ("U", ct.c_double), ("eps", ct.c_double), ("omega", ct.c_double),
+                ("Kx", ct.c_int32), ("Ky", ct.c_int32), ("A", ct.c_double), ("B", ct.c_double), ("C", ct.c_double)]
 PTF_REQ_QUEUED, PTF_REQ_ACTIVE, PTF_REQ_DONE, PTF_REQ_FAILED = 0, 1, 2, 3
 
 
@@ -134,6 +139,7 @@ SIGNATURES = {
     "ptf_server_get_stats": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfServerStats)]),
     "ptf_set_schedule": (ct.c_int, [ct.c_void_p, ct.c_int32, ct.c_int32, ct.c_int32]),
     "ptf_set_flow_layers": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int32]),
+    "ptf_set_flow_analytic": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfFlowDesc)]),
     "ptf_get_tuning": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfTuning)]),
     "ptf_set_tuning": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfTuning)]),
     "ptf_autotune": (ct.c_int, [ct.c_void_p, ct.c_int32, ct.c_int32]),

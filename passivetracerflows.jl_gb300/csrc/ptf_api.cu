@@ -120,6 +120,8 @@ struct ptf_handle {
   bool etd = false;         // ETDRK4 (plain or filtered)
   bool filtered = false;    // Filtered steppers: the state is multiplied by `filt` after each step
   bool flow_layers = false; // one flow per solve (ptf_set_flow_layers)
+  bool flow_tv = false;     // analytic flow re-evaluated at clock.t before each step
+  ptf_flow_desc fdesc{};    // the analytic flow (ptf_set_flow_analytic)
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   // device buffers (compute precision)
@@ -618,6 +620,14 @@ void drop_graph(ptf_handle* h) {
   h->graph_group = -1;
 }
 
+template <typename T> cudaError_t eval_flow(ptf_handle* h, double t) {
+  const double sc = -1.0 / (2.0 * (double)h->nphys);
+  const ptf_config& c = h->cfg;
+  h->launches++;
+  return launch_flow_analytic<T>((T*)h->u, (T*)h->v, (T*)h->w, h->nx, h->ny, h->nz, c.Lx, h->dim >= 2 ? c.Ly : 1.0,
+                                 h->dim == 3 ? c.Lz : 1.0, h->fdesc, t, sc, h->stream);
+}
+
 template <typename T> int do_steps(ptf_handle* h, long long nsteps) {
   if (!h->ab_valid && h->dim >= 2) { int rc = do_prologue<T>(h); if (rc) return rc; }
   int group = h->group > 0 ? std::min(h->group, (int)h->cfg.batch) : auto_group(h);
@@ -646,6 +656,10 @@ template <typename T> int do_steps(ptf_handle* h, long long nsteps) {
   }
   const int per_step = h->dim == 1 ? 4 : (int)(((h->cfg.batch + group - 1) / group) * 4 * (h->dim == 3 ? 4 : 2));
   for (long long n = 0; n < nsteps; ++n) {
+    if (h->flow_tv) {  // the analytic flow at clock.t, frozen for the step's four stages
+      cudaError_t e = eval_flow<T>(h, h->t);
+      if (e != cudaSuccess) return cuda_fail(h, e, "flow evaluation");
+    }
     if (graph) {
       cudaError_t e = cudaGraphLaunch(h->gexec, h->stream);
       if (e != cudaSuccess) return cuda_fail(h, e, "graph launch");
@@ -1092,6 +1106,29 @@ int ptf_set_flow_arrays(ptf_handle* h, const double* u, const double* v, const d
     if (rc) return rc;
   }
   h->flow_layers = false;
+  h->flow_tv = false;
+  h->have_flow = true;
+  return PTF_OK;
+}
+
+int ptf_set_flow_analytic(ptf_handle* h, const ptf_flow_desc* d) {
+  if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
+  if (!d) return fail(h, PTF_ERR_ARG, "null flow description");
+  if (d->kind == PTF_FLOW_CELLULAR) {
+    if (h->dim != 2) return fail(h, PTF_ERR_ARG, "the cellular flow is 2D");
+  } else if (d->kind == PTF_FLOW_ABC) {
+    if (h->dim != 3) return fail(h, PTF_ERR_ARG, "the ABC flow is 3D");
+  } else {
+    return fail(h, PTF_ERR_ARG, "flow kind must be PTF_FLOW_CELLULAR or PTF_FLOW_ABC");
+  }
+  const double vals[6] = {d->U, d->eps, d->omega, d->A, d->B, d->C};
+  for (double x : vals)
+    if (!std::isfinite(x)) return fail(h, PTF_ERR_ARG, "flow parameters must be finite");
+  h->fdesc = *d;
+  h->flow_layers = false;
+  h->flow_tv = d->kind == PTF_FLOW_CELLULAR && d->eps != 0.0 && d->omega != 0.0;
+  cudaError_t e = h->fp32 ? eval_flow<float>(h, h->t) : eval_flow<double>(h, h->t);
+  if (e != cudaSuccess) return cuda_fail(h, e, "flow evaluation");
   h->have_flow = true;
   return PTF_OK;
 }
@@ -1133,6 +1170,7 @@ int ptf_set_flow_layers(ptf_handle* h, const double* u, const double* v, const d
     }
   }
   h->flow_layers = true;
+  h->flow_tv = false;
   h->have_flow = true;
   return PTF_OK;
 }
@@ -1212,6 +1250,10 @@ int ptf_calcN(ptf_handle* h, const double* sol, double* N, int32_t where) {
   // the handle's solution is untouched; the intermediates are recomputed by
   // the next step.
   void* sbuf = h->acc;
+  if (h->flow_tv) {  // calcN! evaluates a time-varying flow at clock.t
+    cudaError_t e = h->fp32 ? eval_flow<float>(h, h->t) : eval_flow<double>(h, h->t);
+    if (e != cudaSuccess) return cuda_fail(h, e, "flow evaluation");
+  }
   int rc = spec_in(h, sol, where, sbuf);
   if (!rc) rc = h->fp32 ? calcN_impl<float>(h, sbuf) : calcN_impl<double>(h, sbuf);
   if (rc) return rc;

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include "ptf_passes.cuh"
 #include "ptf_pass1d.cuh"
+#include "../../include/ptf.h"
 
 #include <string>
 
@@ -44,6 +45,10 @@ cudaError_t launch_solve_sums(const Tin* x, long long n, int batch, double* part
 // k0[4b] = Re src[b * per_solve]; dst[b * per_solve] = (k0[4b], 0)
 cudaError_t launch_k0_from_spec(const double2* src, long long per_solve, int batch, double* k0, cudaStream_t st);
 cudaError_t launch_k0_to_spec(double2* dst, long long per_solve, int batch, const double* k0, cudaStream_t st);
+// analytic flows (ptf_set_flow_analytic) evaluated at time t, pre-scaled
+template <typename T>
+cudaError_t launch_flow_analytic(T* u, T* v, T* w, int nx, int ny, int nz, double Lx, double Ly, double Lz,
+                                 const ptf_flow_desc& d, double t, double scale, cudaStream_t st);
 // per-solve flows: dst[b n + i] = (src[b n + i] + U[b]) * scale (U may be null)
 template <typename T>
 cudaError_t launch_layers_in(const double* src, T* dst, long long n, int batch, const double* U, double scale,

@@ -1,6 +1,7 @@
 // Element conversion kernels between the FP64 user layout and the
 // compute-precision internal layout.
 #include "ptf_internal.h"
+#include "../../include/ptf.h"
 
 namespace ptf {
 
@@ -180,6 +181,43 @@ cudaError_t launch_layers_in(const double* src, T* dst, long long n, int batch, 
   layers_in_kernel<T><<<dim3(gx < 1 ? 1 : gx, batch), 256, 0, st>>>(src, dst, n, U, scale);
   return cudaGetLastError();
 }
+// Analytic flows on the grid x_i = -L/2 + i L/n, pre-scaled like the array
+// flows (scale = -1/(2 points)); FP64 evaluation, stored in T.
+// kind 1 (cellular, 2D): u = U ky cos(kx x + phi) sin(ky y), v = -U kx sin(kx x + phi) cos(ky y),
+//   phi = eps sin(omega t); kind 2 (ABC, 3D).
+template <typename T>
+__global__ void flow_analytic_kernel(T* __restrict__ u, T* __restrict__ v, T* __restrict__ w, int nx, int ny, int nz,
+                                     double Lx, double Ly, double Lz, ptf_flow_desc d, double t, double scale) {
+  const long long n = (long long)nx * ny * nz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int ix = (int)(i % nx);
+    const long long r = i / nx;
+    const int iy = (int)(r % ny), iz = (int)(r / ny);
+    const double x = -Lx / 2 + Lx / nx * ix, y = -Ly / 2 + Ly / ny * iy, z = -Lz / 2 + Lz / nz * iz;
+    if (d.kind == PTF_FLOW_CELLULAR) {
+      const double kx = d.Kx * 2 * M_PI / Lx, ky = d.Ky * 2 * M_PI / Ly;
+      const double arg = kx * x + d.eps * sin(d.omega * t);
+      u[i] = (T)(scale * d.U * ky * cos(arg) * sin(ky * y));
+      v[i] = (T)(scale * -d.U * kx * sin(arg) * cos(ky * y));
+    } else {
+      u[i] = (T)(scale * (d.A * sin(z) + d.C * cos(y)));
+      v[i] = (T)(scale * (d.B * sin(x) + d.A * cos(z)));
+      w[i] = (T)(scale * (d.C * sin(y) + d.B * cos(x)));
+    }
+  }
+}
+template <typename T>
+cudaError_t launch_flow_analytic(T* u, T* v, T* w, int nx, int ny, int nz, double Lx, double Ly, double Lz,
+                                 const ptf_flow_desc& d, double t, double scale, cudaStream_t st) {
+  flow_analytic_kernel<T><<<grid_for((long long)nx * ny * nz), 256, 0, st>>>(u, v, w, nx, ny, nz, Lx, Ly, Lz, d, t,
+                                                                              scale);
+  return cudaGetLastError();
+}
+template cudaError_t launch_flow_analytic<float>(float*, float*, float*, int, int, int, double, double, double,
+                                                 const ptf_flow_desc&, double, double, cudaStream_t);
+template cudaError_t launch_flow_analytic<double>(double*, double*, double*, int, int, int, double, double, double,
+                                                  const ptf_flow_desc&, double, double, cudaStream_t);
+
 template cudaError_t launch_layers_in<float>(const double*, float*, long long, int, const double*, double, cudaStream_t);
 template cudaError_t launch_layers_in<double>(const double*, double*, long long, int, const double*, double, cudaStream_t);
 

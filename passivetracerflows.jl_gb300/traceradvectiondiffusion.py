@@ -322,6 +322,22 @@ class Problem:
             ptrs.append(None)
         L.check(L.load().ptf_set_flow_arrays(self._h, ptrs[0], ptrs[1], ptrs[2], where), self._h)
 
+    def set_flow_analytic(self, kind, **p):
+        """A flow given by formula, evaluated on the device (``ptf_set_flow_analytic``):
+        ``"cellular"`` (2D; ψ = U cos(Kx x + eps sin(omega t)) cos(Ky y), u = -∂ψ/∂y,
+        v = ∂ψ/∂x; re-evaluated at ``clock.t`` before every step when eps and
+        omega are non-zero) or ``"abc"`` (3D; A, B, C).  Replaces the flow the
+        problem was built with; ``stepforward`` then evaluates nothing on the host."""
+        d = L.PtfFlowDesc()
+        d.kind = {"cellular": L.PTF_FLOW_CELLULAR, "abc": L.PTF_FLOW_ABC}[kind]
+        d.U, d.eps, d.omega = float(p.pop("U", 1.0)), float(p.pop("eps", 0.0)), float(p.pop("omega", 0.0))
+        d.Kx, d.Ky = int(p.pop("Kx", 1)), int(p.pop("Ky", 1))
+        d.A, d.B, d.C = float(p.pop("A", 1.0)), float(p.pop("B", math.sqrt(2 / 3))), float(p.pop("C", math.sqrt(1 / 3)))
+        if p:
+            raise TypeError(f"unexpected flow parameters: {sorted(p)}")
+        L.check(L.load().ptf_set_flow_analytic(self._h, ct.byref(d)), self._h)
+        self._device_flow = True
+
     def _refresh_flow(self):
         """Time-varying flow at ``clock.t`` (``:715-718``), evaluated once per step."""
         t = self.clock.t
@@ -351,7 +367,7 @@ class Problem:
         shape = ((self.batch,) if self.batch > 1 else ()) + self.grid.spec_shape
         a = np.ascontiguousarray(np.broadcast_to(np.asarray(sol, dtype=np.complex128), shape))
         out = np.empty(shape, dtype=np.complex128)
-        if not self.flow.steadyflow:
+        if not self.flow.steadyflow and not getattr(self, "_device_flow", False):
             self._refresh_flow()
         L.check(L.load().ptf_calcN(self._h, a.ctypes.data_as(ct.c_void_p), out.ctypes.data_as(ct.c_void_p),
                                    L.PTF_HOST), self._h)
@@ -441,7 +457,7 @@ def stepforward(prob: Problem, nsteps: int = 1):
     if nsteps < 0:
         raise ValueError("nsteps must be non-negative")
     lib = L.load()
-    if prob.flow.steadyflow:
+    if prob.flow.steadyflow or getattr(prob, "_device_flow", False):
         L.check(lib.ptf_step(prob._h, nsteps), prob._h)
         return
     for _ in range(nsteps):

@@ -187,3 +187,58 @@ def test_golden_etdrk4_fp64_fp32(gpu, oracle):
         gpu.set_c(p, gauss(x, y))
         gpu.stepforward(p, 50); gpu.updatevars(p)
         assert oracle.rel_l2(p.vars.c, g["c50"]) <= tol, T
+
+
+@pytest.mark.parametrize("T,tol", [(np.float64, 1e-12), (np.float32, 1e-5)])
+def test_analytic_cellular_flow_on_device(gpu, oracle, T, tol):
+    """ptf_set_flow_analytic: the time-dependent cellular flow evaluated on the
+    device at clock.t before every step equals the same flow given as a Python
+    function (evaluated on the host at clock.t) -- and the oracle."""
+    U, eps, om, Kx, Ky = 0.8, 0.4, 3.0, 2, 1
+    k, l = float(Kx), float(Ky)
+    u = lambda x, y, t: U * l * np.cos(k * x + eps * np.sin(om * t)) * np.sin(l * y)  # noqa: E731
+    v = lambda x, y, t: -U * k * np.sin(k * x + eps * np.sin(om * t)) * np.cos(l * y)  # noqa: E731
+    kw = dict(nx=128, dt=0.004, stepper="RK4")
+    p = gpu.Problem(gpu.GPU(), gpu.TwoDAdvectingFlow(), κ=1e-3, T=T, **kw)
+    p.set_flow_analytic("cellular", U=U, eps=eps, omega=om, Kx=Kx, Ky=Ky)
+    q = gpu.Problem(gpu.GPU(), gpu.TwoDAdvectingFlow(u=u, v=v, steadyflow=False), κ=1e-3, T=T, **kw)
+    r = oracle.Problem(oracle.TwoDAdvectingFlow(u=u, v=v, steadyflow=False), kappa=1e-3, **kw)
+    x, y = gpu.gridpoints(p.grid)
+    c0 = gauss(x, y, 0.2, -0.5, 0.4)
+    for prob in (p, q):
+        gpu.set_c(prob, c0)
+        gpu.stepforward(prob, 25)
+        gpu.updatevars(prob)
+    oracle.set_c(r, c0)
+    oracle.stepforward(r, 25)
+    oracle.updatevars(r)
+    assert oracle.rel_l2(p.vars.c, q.vars.c) <= (1e-13 if T is np.float64 else 1e-6)
+    assert oracle.rel_l2(p.vars.c, r.vars.c) <= tol
+    # calcN! at clock.t with the device-evaluated flow
+    N = p.calcN(p.sol)
+    Nr = np.zeros_like(r.sol)
+    oracle.calcN(Nr, r.sol, r.clock.t, r.clock, r.params, r.grid)
+    if T is np.float64:
+        assert oracle.rel_l2(N, Nr) <= 1e-12
+
+
+def test_analytic_abc_flow_on_device(gpu, oracle):
+    A, B, C = 1.0, np.sqrt(2 / 3), np.sqrt(1 / 3)
+    fu = lambda x, y, z: A * np.sin(z) + C * np.cos(y)  # noqa: E731
+    fv = lambda x, y, z: B * np.sin(x) + A * np.cos(z)  # noqa: E731
+    fw = lambda x, y, z: C * np.sin(y) + B * np.cos(x)  # noqa: E731
+    kw = dict(nx=32, dt=0.005, stepper="ETDRK4")
+    p = gpu.Problem(gpu.GPU(), gpu.ThreeDAdvectingFlow(), κ=5e-4, **kw)
+    p.set_flow_analytic("abc", A=A, B=B, C=C)
+    r = oracle.Problem(oracle.ThreeDAdvectingFlow(u=fu, v=fv, w=fw), kappa=5e-4, **kw)
+    x, y, z = gpu.gridpoints(p.grid)
+    c0 = np.exp(-(x ** 2 + y ** 2 + z ** 2) / (2 * 0.3 ** 2))
+    gpu.set_c(p, c0)
+    oracle.set_c(r, c0)
+    gpu.stepforward(p, 10)
+    oracle.stepforward(r, 10)
+    gpu.updatevars(p)
+    oracle.updatevars(r)
+    assert oracle.rel_l2(p.vars.c, r.vars.c) <= 1e-12
+    with pytest.raises(Exception):
+        p.set_flow_analytic("cellular")  # the cellular flow is 2D
