@@ -373,6 +373,32 @@ class Problem:
                                    L.PTF_HOST), self._h)
         return out
 
+    def save_state(self, path):
+        """Checkpoint: ``sol`` (FP64, including the FP64 k = 0 mode of FP32
+        problems) and the clock, to a NumPy ``.npz`` -- what the reference's
+        JLD2 output records of a solve (``saveoutput``; the examples save
+        ``sol`` and ``clock.t``).  ``load_state`` resumes bit-identically."""
+        t, step = self.clock._read()
+        cfg = self._cfg
+        with open(path, "wb") as f:  # exactly at ``path`` (np.savez would append ".npz")
+            np.savez(f, sol=self.sol, t=t, step=step, dim=cfg.dim, nx=cfg.nx, ny=cfg.ny, nz=cfg.nz,
+                     batch=cfg.batch, dt=cfg.dt, stepper=cfg.stepper, precision=cfg.precision)
+
+    def load_state(self, path):
+        """Resume from ``save_state``: the grid, batch, dt, stepper and
+        precision must match this problem."""
+        with np.load(path) as z:
+            cfg = self._cfg
+            for k in ("dim", "nx", "ny", "nz", "batch", "stepper", "precision"):
+                if int(z[k]) != int(getattr(cfg, k)):
+                    raise ValueError(f"checkpoint {k}={int(z[k])} does not match this problem ({getattr(cfg, k)})")
+            if float(z["dt"]) != cfg.dt:
+                raise ValueError("checkpoint dt does not match this problem")
+            self.sol = z["sol"]
+            L.check(L.load().ptf_set_clock(self._h, float(z["t"]), int(z["step"])), self._h)
+        if not self.flow.steadyflow and not getattr(self, "_device_flow", False):
+            self._flow_t = None
+
     def set_schedule(self, solves_per_group=0, branches=1, use_graph=True):
         """Step a batch in groups of solves (0: whole batch, or batch/branches),
         dealt to `branches` concurrent stream branches, replaying steps from a
