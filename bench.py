@@ -492,7 +492,7 @@ def run_ours(args):
     e2e_val = job_rate(world, B * n * n * frames * S, e2e_s)
     bytes_field = B * n * n * 8
     # ---------------- other configurations (rank 0, bounded) ----------------
-    configs = {}
+    workloads = {}
     if rank == 0 and not args.only_main:
         for key, fn in (("3d_abc_256", lambda: run_abc3d_256(pkg, torch)),
                         ("ensemble_256_solves", lambda: run_ensemble_256(pkg, torch, args.ensemble_steps)),
@@ -502,9 +502,9 @@ def run_ours(args):
                         ("served_fp64", lambda: run_served_stream(pkg, np.float64, args.serve_requests_fp64,
                                                             args.serve_rate / 4))):
             try:
-                configs[key] = fn()
+                workloads[key] = fn()
             except Exception as e:  # report the failure in the line rather than losing the main result
-                configs[key] = {"error": f"{type(e).__name__}: {e}"}
+                workloads[key] = {"error": f"{type(e).__name__}: {e}"}
     # ---------------- CPU baseline (rank 0) ----------------
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -550,10 +550,10 @@ def run_ours(args):
                 "api": f"set_c(pinned host) + {frames} x (stepforward({S}) + updatevars(pinned host))"},
         "gpu_launches": launches,
         "clocks": clocks,
-        "serving": ({k: configs["served_fp32"].get(k) for k in ("p50_latency_s", "p99_latency_s", "grid_pt_steps_per_s",
+        "serving": ({k: workloads["served_fp32"].get(k) for k in ("p50_latency_s", "p99_latency_s", "grid_pt_steps_per_s",
                                                                "requests", "completed")}
-                    if "served_fp32" in configs else None),
-        "configs": configs,
+                    if "served_fp32" in workloads else None),
+        "workloads": workloads,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
