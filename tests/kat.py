@@ -134,6 +134,37 @@ def hyperdiffusion(api, dev, stepper="RK4", dt=0.005, tfinal=0.1):
     return _rel(cf, prob.vars.c), 128 * 128 * nsteps * 1e-12
 
 
+def diffusion_multilayerqg(api, dev, stepper="RK4", dt=0.005, tfinal=0.1):
+    """test_diffusion_multilayerqg (:303-351): a MultiLayerQG problem at rest
+    (q = 0, U = 0; 2 layers on 128², stepped to the tracer release time 50 dt),
+    each layer's tracer diffusing a Gaussian with κ = η = 0.01; the reference
+    checks both layers against the heat kernel at n²·nsteps·1e-12."""
+    nsteps = round(tfinal / dt)
+    nl, n, L, κ, s = 2, 128, 2 * np.pi, 0.01, 0.1
+    if dev is None:
+        prob = api.MultiLayerProblem(nx=n, Lx=L, nlayers=nl, dt=dt, kappa=κ, stepper=stepper)
+        prob.set_layer_flows(np.zeros((nl, n, n)), np.zeros((nl, n, n)), np.zeros(nl))
+        x, y = prob.grid.gridpoints()
+    else:
+        released = []
+        mq = api.MultiLayerQGFlow(nx=n, Lx=L, nlayers=nl, dt=dt, U=np.zeros(nl),
+                                  step_until=lambda m, t: released.append(t))  # the QG state stays at rest
+        prob = api.Problem(mq, κ=κ, stepper=stepper, tracer_release_time=50 * dt)
+        assert released == [50 * dt] and prob.clock.t == 0.0
+        x, y = api.gridpoints(prob.grid)
+    c0 = np.stack([0.1 * np.exp(-(x ** 2 + y ** 2) / (2 * s ** 2))] * nl)
+    if dev is None:
+        prob.set_c(c0); prob.stepforward(nsteps); prob.updatevars()
+        c = prob.c
+    else:
+        api.set_c(prob, c0); api.stepforward(prob, nsteps); api.updatevars(prob)
+        c = prob.vars.c
+    tf = nsteps * dt
+    st = np.sqrt(2 * κ * tf + s ** 2)
+    cf = 0.1 * (s ** 2 / st ** 2) * np.exp(-(x ** 2 + y ** 2) / (2 * st ** 2))
+    return max(_rel(cf, c[j]) for j in range(nl)), n * n * nsteps * 1e-12
+
+
 def constvel3D(api, dev, stepper="RK4", dt=1e-2, nsteps=40, n=128):
     """test_constvel3D (:155-182)."""
     uvel, vvel, wvel = 0.2, 0.1, 0.05

@@ -45,3 +45,11 @@ def test_reference_kat_3d_gpu(gpu, name, tight):
 def test_reference_kat_diffusion3D_gpu(gpu, steadyflow):
     err, rtol = kat.diffusion3D(gpu, gpu.GPU(), steadyflow=steadyflow)
     assert err <= rtol and err <= 4.1e-4
+
+
+@pytest.mark.parametrize("stepper,tight", [("RK4", 1e-9), ("ETDRK4", 1e-11)])
+def test_reference_kat_diffusion_multilayerqg_gpu(gpu, stepper, tight):
+    """test_diffusion_multilayerqg through Problem(MQGprob; ...) (the layers
+    are the solves of one batched handle)."""
+    err, rtol = kat.diffusion_multilayerqg(gpu, gpu.GPU(), stepper=stepper)
+    assert err <= rtol and err <= tight

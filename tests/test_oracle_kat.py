@@ -37,6 +37,16 @@ def test_diffusion2D_timevarying(oracle):
     assert err <= rtol and err <= 1e-9
 
 
+@pytest.mark.parametrize("stepper,tight", [("RK4", 1e-9), ("ETDRK4", 1e-11)])
+def test_diffusion_multilayerqg(oracle, stepper, tight):
+    """test/runtests.jl:50-52 runs it with stepper "RK4" (ETDRK4, exact for
+    diffusion, lands at round-off).  The Filtered steppers would not pass it:
+    the filter damps the Gaussian's modes above 0.65 of the Nyquist
+    wavenumber, a 3.5e-6 error against the 3.3e-7 tolerance."""
+    err, rtol = kat.diffusion_multilayerqg(oracle, None, stepper=stepper)
+    assert err <= rtol and err <= tight
+
+
 def test_clock_t_freeze_is_what_the_reference_tests_pin(oracle):
     """The reference evaluates a time-varying flow at clock.t for all stages
     (src/traceradvectiondiffusion.jl:718); test_timedependentvel2D only passes
