@@ -397,8 +397,13 @@ class MultiLayerProblem:
         return np.stack([pr.vars.c for pr in self.layers])
 
     def set_c(self, c):
+        """``set_c!`` (``:861-870``): one 2D field repeated over the layers (a
+        stack of per-layer fields is taken as it is)."""
+        c = np.asarray(c, dtype=np.float64)
+        if c.ndim == 2:
+            c = np.broadcast_to(c, (self.nlayers,) + c.shape)
         for j, pr in enumerate(self.layers):
-            set_c(pr, np.asarray(c)[j])
+            set_c(pr, c[j])
 
     def stepforward(self, nsteps=1):
         for pr in self.layers:

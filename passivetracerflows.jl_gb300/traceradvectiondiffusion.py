@@ -202,6 +202,28 @@ def _kw(kwargs, names, default):
     return default
 
 
+def _is_device(a):
+    return hasattr(a, "is_cuda") and a.is_cuda
+
+
+def _device_array(a, numel, what):
+    """A CUDA tensor handed to the library by pointer: the library reads
+    exactly ``numel`` float64 values from it, so anything else is refused."""
+    import torch
+    if a.dtype != torch.float64 or not a.is_contiguous():
+        raise ValueError(f"{what}: device arrays must be contiguous float64 tensors")
+    if a.numel() != numel:
+        raise ValueError(f"{what}: {a.numel()} values on the device, {numel} expected")
+    return a
+
+
+def _all_host_or_device(arrays, what):
+    dev = [_is_device(a) for a in arrays]
+    if any(dev) and not all(dev):
+        raise ValueError(f"{what}: pass all arrays on the host or all on the device, not a mix")
+    return all(dev) and len(dev) > 0
+
+
 def _eval_on_grid(f, shape, pts, *extra):
     return np.ascontiguousarray(np.broadcast_to(np.asarray(f(*pts, *extra), dtype=np.float64), shape))
 
@@ -307,12 +329,13 @@ class Problem:
     def set_flow_arrays(self, *vel):
         """Set the flow from grid arrays (host NumPy or torch CUDA tensors)."""
         arrs = []
-        where = L.PTF_HOST
         ptrs = []
+        on_device = _all_host_or_device(vel, "set_flow_arrays")
+        where = L.PTF_DEVICE if on_device else L.PTF_HOST
+        npts = math.prod(self.grid.shape)
         for a in vel:
-            if hasattr(a, "is_cuda") and a.is_cuda:
-                where = L.PTF_DEVICE
-                ptrs.append(ct.c_void_p(a.data_ptr()))
+            if on_device:
+                ptrs.append(ct.c_void_p(_device_array(a, npts, "set_flow_arrays").data_ptr()))
                 arrs.append(a)
             else:
                 a = np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64), self.grid.shape))
@@ -457,9 +480,13 @@ class Problem:
 
 def set_c(prob: Problem, c):
     """``set_c!(prob, c)`` (``:844-852, :872``): ``sol = rfft(c)``, then ``updatevars!``."""
-    if hasattr(c, "is_cuda") and c.is_cuda:
-        if c.dtype != __import__("torch").float64 or not c.is_contiguous():
-            raise ValueError("device fields must be contiguous float64 tensors")
+    if _is_device(c):
+        npts = math.prod(prob.grid.shape)
+        if prob.batch > 1 and c.numel() == npts:
+            # one field for every solve of the batch (for a MultiLayerQG
+            # problem: every layer, as set_c! repeats c, :861-870)
+            c = c.reshape(prob.grid.shape).expand((prob.batch,) + prob.grid.shape).contiguous()
+        c = _device_array(c, prob.batch * npts, "set_c")
         L.check(L.load().ptf_set_c(prob._h, ct.c_void_p(c.data_ptr()), L.PTF_DEVICE), prob._h)
     else:
         shape = ((prob.batch,) if prob.batch > 1 else ()) + prob.grid.shape
@@ -573,11 +600,12 @@ class MultiLayerTracerProblem(Problem):
         mq = self.MQGprob
         U = np.asarray(getattr(mq.params, "U", np.zeros(self.nlayers)), dtype=np.float64).reshape(self.nlayers)
         shape = (self.nlayers,) + self.grid.shape
-        ptrs, keep, where = [], [], L.PTF_HOST
+        ptrs, keep = [], []
+        on_device = _all_host_or_device((mq.vars.u, mq.vars.v), "MQGprob.vars.u, v")
+        where = L.PTF_DEVICE if on_device else L.PTF_HOST
         for a in (mq.vars.u, mq.vars.v):
-            if hasattr(a, "is_cuda") and a.is_cuda:
-                where = L.PTF_DEVICE
-                ptrs.append(ct.c_void_p(a.data_ptr()))
+            if on_device:
+                ptrs.append(ct.c_void_p(_device_array(a, math.prod(shape), "MQGprob.vars.u, v").data_ptr()))
                 keep.append(a)
             else:
                 a = np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64), shape))

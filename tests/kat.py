@@ -152,7 +152,7 @@ def diffusion_multilayerqg(api, dev, stepper="RK4", dt=0.005, tfinal=0.1):
         prob = api.Problem(mq, κ=κ, stepper=stepper, tracer_release_time=50 * dt)
         assert released == [50 * dt] and prob.clock.t == 0.0
         x, y = api.gridpoints(prob.grid)
-    c0 = np.stack([0.1 * np.exp(-(x ** 2 + y ** 2) / (2 * s ** 2))] * nl)
+    c0 = 0.1 * np.exp(-(x ** 2 + y ** 2) / (2 * s ** 2))  # one 2D field: set_c! repeats it over the layers
     if dev is None:
         prob.set_c(c0); prob.stepforward(nsteps); prob.updatevars()
         c = prob.c

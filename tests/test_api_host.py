@@ -84,3 +84,39 @@ def test_multilayer_dispatch_and_arguments(pkg):
     with pytest.raises(Exception):  # no GPU here: fails at the device, after stepping the flow
         pkg.Problem(mq2, tracer_release_time=0.25)
     assert seen == [0.25]
+
+
+def test_device_arrays_are_checked_before_the_library_reads_them(pkg):
+    """The library reads exactly the problem's number of float64 values from
+    a device pointer: wrong dtype, layout or size is refused on the host
+    (checked here on CPU tensors, which take the same checks)."""
+    torch = pytest.importorskip("torch")
+    from ptf_gb300 import traceradvectiondiffusion as tad
+    ok = torch.zeros(3, 8, dtype=torch.float64)
+    assert tad._device_array(ok, 24, "u") is ok
+    with pytest.raises(ValueError, match="float64"):
+        tad._device_array(torch.zeros(24, dtype=torch.float32), 24, "u")
+    with pytest.raises(ValueError, match="contiguous"):
+        tad._device_array(ok.t(), 24, "u")
+    with pytest.raises(ValueError, match="23 values"):
+        tad._device_array(torch.zeros(23, dtype=torch.float64), 24, "u")
+
+
+def test_host_and_device_arrays_are_not_mixed(pkg):
+    from ptf_gb300 import traceradvectiondiffusion as tad
+
+    class OnDevice:
+        is_cuda = True
+
+    assert tad._all_host_or_device((np.zeros(2), np.zeros(2)), "u, v") is False
+    assert tad._all_host_or_device((OnDevice(), OnDevice()), "u, v") is True
+    with pytest.raises(ValueError, match="mix"):
+        tad._all_host_or_device((np.zeros(2), OnDevice()), "u, v")
+
+
+def test_multilayer_oracle_repeats_one_field_over_layers(oracle):
+    """set_c! of a MultiLayerQG-coupled problem (:861-870) repeats a 2D field."""
+    p = oracle.MultiLayerProblem(nx=16, nlayers=3, dt=0.01, kappa=0.01)
+    c = np.random.default_rng(0).standard_normal((16, 16))
+    p.set_c(c)
+    assert all(np.allclose(p.c[j], c, atol=1e-14) for j in range(3))
