@@ -64,6 +64,16 @@ class AdvectingFlow:
                   3: (self.u, self.v, self.w, self.steadyflow)}[self.dim]
         return iter(fields)
 
+    def __str__(self):  # Base.show (``:110-125``)
+        names = ("u", "v", "w")[: self.dim]
+        kind = {1: "OneD", 2: "TwoD", 3: "ThreeD"}[self.dim] + "AdvectingFlow"
+        lines = [kind] + [f"  ├────────── {n}: {_summary(getattr(self, n))}" for n in names]
+        return "\n".join(lines + [f"  └─ steadyflow: {str(self.steadyflow).lower()}"])
+
+
+def _summary(f):
+    return getattr(f, "__name__", type(f).__name__)
+
 
 def OneDAdvectingFlow(*, u=noflow, steadyflow=True):
     """``OneDAdvectingFlow(; u=noflow, steadyflow=true)`` (``:54``)."""

@@ -120,3 +120,15 @@ def test_multilayer_oracle_repeats_one_field_over_layers(oracle):
     c = np.random.default_rng(0).standard_normal((16, 16))
     p.set_c(c)
     assert all(np.allclose(p.c[j], c, atol=1e-14) for j in range(3))
+
+
+def test_flow_display(pkg):
+    """Base.show of the flow containers (src/traceradvectiondiffusion.jl:110-125)."""
+    def cellu(x, y):
+        return 0.0
+    s = str(pkg.TwoDAdvectingFlow(u=cellu, steadyflow=False)).splitlines()
+    assert s[0] == "TwoDAdvectingFlow"
+    assert s[1] == "  ├────────── u: cellu" and s[2] == "  ├────────── v: noflow"
+    assert s[3] == "  └─ steadyflow: false"
+    assert len(str(pkg.ThreeDAdvectingFlow()).splitlines()) == 5
+    assert len(str(pkg.OneDAdvectingFlow()).splitlines()) == 3
