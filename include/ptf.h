@@ -122,7 +122,11 @@ int ptf_set_flow_layers(ptf_handle* h, const double* u, const double* v, const d
 int ptf_set_c(ptf_handle* h, const double* c, int32_t where);
 /* updatevars!(prob) then copy vars.c out (:815-821, :837). */
 int ptf_get_c(ptf_handle* h, double* c, int32_t where);
-/* prob.sol out / in (complex, (nx/2+1)*ny[*nz] per solve). */
+/* prob.sol out / in (complex, (nx/2+1)*ny[*nz] per solve).  For FP32
+ * handles with k0_mode, get_sol reports the FP64 k = 0 mode and set_sol
+ * seeds it, so get_sol then set_sol (with ptf_clock / ptf_set_clock) saves
+ * and resumes a solve exactly -- the state a FourierFlows snapshot of
+ * sol and clock holds. */
 int ptf_get_sol(ptf_handle* h, double* sol, int32_t where);
 int ptf_set_sol(ptf_handle* h, const double* sol, int32_t where);
 
@@ -199,8 +203,9 @@ int32_t ptf_abi_version(void);
  * problems (each with its own grid size, diffusivity, dt, clock, step count
  * and flow) together.  Square 2D grids n in {64, 128, 256, 512, 1024}, RK4
  * (FourierFlows RK4 on the same L and calcN! as ptf_step).  Each stage of
- * all solves is one persistent kernel launch; a step is replayed from a
- * captured CUDA graph.
+ * all solves is a row launch and a column launch over every solve's work
+ * items (or one persistent launch, ptf_batch_config.persistent); a step is
+ * replayed from a captured CUDA graph.
  * ------------------------------------------------------------------------- */
 enum ptf_flow_kind {
   PTF_FLOW_ARRAYS = 0,   /* steady flow given as grid arrays u, v */
