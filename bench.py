@@ -282,6 +282,17 @@ def replica_seed(rank, base=1234):
     return base + rank
 
 
+# A rank that dies (or never reaches a collective) ends the others' next
+# collective with an error after this long, instead of the backend's default.
+PG_TIMEOUT_S = 300
+
+
+def init_ranks(backend, timeout_s=PG_TIMEOUT_S):
+    import datetime
+    import torch.distributed as dist
+    dist.init_process_group(backend, timeout=datetime.timedelta(seconds=timeout_s))
+
+
 def max_over_ranks(x, world, device):
     """Largest value of x over the ranks (the job's time is its slowest rank's)."""
     if world == 1:
@@ -329,8 +340,7 @@ def run_ours(args):
     import torch
     world, rank, local = dist_setup()
     if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+        init_ranks("nccl")
     torch.cuda.set_device(local)
     import __graft_entry__ as g
     lib_path = g.PKG_DIR / "libptf.so"

@@ -32,8 +32,8 @@ def _rank_main(rank, world, port, out_dir):
     import torch.distributed as dist
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
                       LOCAL_RANK=str(rank))
-    dist.init_process_group("gloo", rank=rank, world_size=world)
     b = _bench()
+    b.init_ranks("gloo")
     w, r, local = b.dist_setup()
     seed = b.replica_seed(r)
     c0 = b.initial_conditions(32, 2, seed)
@@ -61,6 +61,43 @@ def test_two_gloo_replicas(tmp_path):
     # every rank sees the slowest rank's time, and the job rate uses it
     assert all(x["slowest"] == 1.5 for x in res)
     assert all(abs(x["rate"] - 2 * 2 * 32 * 32 * 10 / 1.5) < 1e-6 for x in res)
+
+
+def _rank_fails(rank, world, port, out_dir, mode):
+    import time
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    b = _bench()
+    b.init_ranks("gloo", timeout_s=5)
+    if rank == 1:
+        if mode == "stalls":  # alive but never reaches the barrier (until rank 0 has given up)
+            t_end = time.monotonic() + 60
+            while not Path(out_dir, "rank0.json").exists() and time.monotonic() < t_end:
+                time.sleep(0.1)
+        return  # "leaves": exits between steps without reaching the barrier
+    t0 = time.monotonic()
+    try:
+        dist.barrier()
+        outcome = "returned"
+    except Exception as e:  # the backend's error for a peer that is gone or late
+        outcome = type(e).__name__
+    Path(out_dir, "rank0.json").write_text(json.dumps({"outcome": outcome, "seconds": time.monotonic() - t0}))
+
+
+@pytest.mark.parametrize("mode", ["leaves", "stalls"])
+def test_a_failed_rank_ends_the_next_collective_with_an_error(tmp_path, mode):
+    """Failure detection on the host: rank 1 exits, or stays alive without
+    reaching the barrier; rank 0's barrier fails with an error (at once for a
+    rank that is gone, after the 5 s process-group timeout for one that
+    stalls) instead of waiting for ever."""
+    pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    mp.start_processes(_rank_fails, args=(2, _free_port(), str(tmp_path), mode), nprocs=2, start_method="spawn",
+                       join=True)
+    r = json.loads((tmp_path / "rank0.json").read_text())
+    assert r["outcome"] != "returned"
+    assert r["seconds"] < 30
 
 
 def test_single_process_defaults():
