@@ -28,6 +28,7 @@
 
 #include "../../include/ptf.h"
 #include "ptf_internal.h"
+#include "ptf_trace.h"
 
 using namespace ptf;
 
@@ -1176,6 +1177,7 @@ int ptf_set_flow_layers(ptf_handle* h, const double* u, const double* v, const d
 }
 
 int ptf_set_c(ptf_handle* h, const double* c, int32_t where) {
+  ptf::TraceRange tr("ptf_set_c");
   if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
   if (!c) return fail(h, PTF_ERR_ARG, "null field");
   if (check_where(h, where)) return PTF_ERR_ARG;
@@ -1190,6 +1192,7 @@ int ptf_set_c(ptf_handle* h, const double* c, int32_t where) {
 }
 
 int ptf_get_c(ptf_handle* h, double* c, int32_t where) {
+  ptf::TraceRange tr("ptf_get_c");
   if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
   if (!c) return fail(h, PTF_ERR_ARG, "null field");
   if (check_where(h, where)) return PTF_ERR_ARG;
@@ -1234,6 +1237,7 @@ int ptf_set_sol(ptf_handle* h, const double* sol, int32_t where) {
 }
 
 int ptf_step(ptf_handle* h, int64_t nsteps) {
+  ptf::TraceRange tr("ptf_step");
   if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
   if (nsteps < 0) return fail(h, PTF_ERR_ARG, "nsteps must be >= 0");
   if (!h->have_flow) return fail(h, PTF_ERR_STATE, "no flow set (ptf_set_flow_arrays)");
@@ -1242,6 +1246,7 @@ int ptf_step(ptf_handle* h, int64_t nsteps) {
 }
 
 int ptf_calcN(ptf_handle* h, const double* sol, double* N, int32_t where) {
+  ptf::TraceRange tr("ptf_calcN");
   if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
   if (!sol || !N) return fail(h, PTF_ERR_ARG, "null field");
   if (!h->have_flow) return fail(h, PTF_ERR_STATE, "no flow set (ptf_set_flow_arrays)");
@@ -1364,6 +1369,7 @@ int ptf_set_tuning(ptf_handle* h, const ptf_tuning* t) {
 }
 
 int ptf_autotune(ptf_handle* h, int32_t trial_steps, int32_t flags) {
+  ptf::TraceRange tr("ptf_autotune");
   if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
   if (trial_steps < 1 || trial_steps > 1000) return fail(h, PTF_ERR_ARG, "trial_steps must be in 1..1000");
   if (!h->have_flow) return fail(h, PTF_ERR_STATE, "no flow set (ptf_set_flow_arrays)");

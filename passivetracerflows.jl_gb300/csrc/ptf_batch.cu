@@ -31,6 +31,7 @@
 
 #include "../../include/ptf.h"
 #include "ptf_batch_kern.cuh"
+#include "ptf_trace.h"
 
 using namespace ptf;
 
@@ -632,6 +633,7 @@ int ptf_batch_add(ptf_batch* b, const ptf_solve_desc* d, const double* c0, const
 }
 
 int ptf_batch_step(ptf_batch* b, int64_t nsteps) {
+  ptf::TraceRange tr("ptf_batch_step");
   if (!b) return bfail(nullptr, PTF_ERR_ARG, "null batch");
   if (nsteps < 0) return bfail(b, PTF_ERR_ARG, "nsteps must be >= 0");
   return b->fp32 ? step_impl<float>(b, nsteps) : step_impl<double>(b, nsteps);
