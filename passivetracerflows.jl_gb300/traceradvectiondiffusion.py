@@ -22,6 +22,7 @@ functions on the grid (as the reference's broadcasts do) and keeps the
 from __future__ import annotations
 
 import ctypes as ct
+import logging
 import math
 from dataclasses import dataclass
 from typing import Callable
@@ -29,6 +30,8 @@ from typing import Callable
 import numpy as np
 
 from . import _lib as L
+
+_log = logging.getLogger("ptf_gb300")
 
 __all__ = [
     "CPU", "GPU", "noflow", "OneDAdvectingFlow", "TwoDAdvectingFlow", "ThreeDAdvectingFlow",
@@ -592,6 +595,7 @@ class MultiLayerTracerProblem(Problem):
         if tracer_release_time < 0:
             raise ValueError("tracer_release_time must be non-negative!")
         if tracer_release_time > 0:
+            _log.info("Stepping the flow forward until t = tracer_release_time = %s", tracer_release_time)
             MQGprob.step_until(tracer_release_time)
         self.MQGprob = MQGprob
         g = MQGprob.grid

@@ -86,6 +86,16 @@ def test_multilayer_dispatch_and_arguments(pkg):
     assert seen == [0.25]
 
 
+def test_tracer_release_is_logged(pkg, caplog):
+    """@info "Stepping the flow forward until t = tracer_release_time = ..." (:237)."""
+    import logging
+    mq = pkg.MultiLayerQGFlow(nx=32, nlayers=2, dt=0.01, step_until=lambda m, t: None)
+    with caplog.at_level(logging.INFO, logger="ptf_gb300"):
+        with pytest.raises(Exception):  # no GPU here
+            pkg.Problem(mq, tracer_release_time=0.25)
+    assert "tracer_release_time = 0.25" in caplog.text
+
+
 def test_device_arrays_are_checked_before_the_library_reads_them(pkg):
     """The library reads exactly the problem's number of float64 values from
     a device pointer: wrong dtype, layout or size is refused on the host
