@@ -16,7 +16,10 @@ Parity status: RK4 is pinned by the reference's analytic known-answer tests.
 ETDRK4 is not exercised by any reference test; its contour-integral
 coefficients follow Kassam & Trefethen (2005) with 32 points on a unit circle
 ("parity unpinned" for ETDRK4 beyond the analytic diffusion limit, where the
-ETDRK4 update is exact and is checked in the tests).
+ETDRK4 update is exact and is checked in the tests).  In place of a reference
+pin, ``tests/test_oracle_etdrk4.py`` checks the coefficients against the
+phi-function closed forms in 100-digit arithmetic and the stepper's fourth-order
+convergence.
 
 Layout: NumPy C order with x the LAST (fastest) axis, i.e. a 2D field has
 shape ``(ny, nx)`` and a 3D field ``(nz, ny, nx)``.  That is byte-for-byte the
