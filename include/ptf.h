@@ -164,14 +164,14 @@ int ptf_set_schedule(ptf_handle* h, int32_t solves_per_group, int32_t branches, 
  * copies (falls back to the direct kernel where that does not fit);
  * col_carveout: the share of the SM's L1/shared storage the column passes
  * ask to be shared memory (the rest caches, among others, register spills;
- * set by hand -- measured no better than the driver's choice, so the tuner
+ * set by hand -- measured no better than the CUDA driver's choice, so the tuner
  * leaves it at -1);
  * ms_per_step: the time measured by ptf_autotune (0 when not tuned).  Line
  * counts are powers of two dividing the lines of the pass, within the
  * block's resource limit.  Shapes do not change results. */
 typedef struct ptf_tuning {
   int32_t col_lines, col_lines_y, row_pairs, branches, solves_per_group, row_staged;
-  int32_t col_carveout; /* column passes' preferred shared-memory carve-out, percent (-1: driver's choice) */
+  int32_t col_carveout; /* column passes' preferred shared-memory carve-out, percent (-1: CUDA driver's choice) */
   double ms_per_step;
 } ptf_tuning;
 enum { PTF_TUNE_FORCE = 1 };

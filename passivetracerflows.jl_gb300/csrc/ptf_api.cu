@@ -99,7 +99,7 @@ template <typename F> void parallel_for(long long n, F f) {
 // stride `stride`, ncols flat columns, nblk_y blocks of fields bstride apart.
 struct ColGeom {
   int n = 0, stride = 0, ncols = 0, nblk_y = 0, W = 1;
-  int carve = -1;  // preferred shared-memory carve-out in percent (-1: the driver's choice)
+  int carve = -1;  // preferred shared-memory carve-out in percent (-1: the CUDA driver's choice)
   long long bstride = 0;
   double dk = 0;
   int axis = 0;  // 1 = y, 2 = z

@@ -14,7 +14,7 @@ void set_global_error(const std::string& msg);
 
 // Pass launchers (ptf_kern2d.cu dispatching to ptf_k2d_inst.cu objects).
 // Column pass over transform length n: grid (nbx, nby), W columns per block.
-// carve: preferred shared-memory carve-out in percent (-1: the driver's choice).
+// carve: preferred shared-memory carve-out in percent (-1: the CUDA driver's choice).
 template <typename T>
 cudaError_t launch_col(int n, const ColArgs<T>& a, int W, int nbx, int nby, cudaStream_t st, int carve = -1);
 // Row pass over x length nx: grid (nbx, batch), P row pairs per block.
