@@ -387,7 +387,14 @@ class MultiLayerProblem:
         self.clock = self.layers[0].clock
 
     def set_layer_flows(self, u, v, U=None):
-        U = np.zeros(self.nlayers) if U is None else np.asarray(U, dtype=np.float64).reshape(self.nlayers)
+        """``u_j + U_j``, ``v_j`` per layer (``:794-795``).  ``U``: one value
+        per layer, or ``(nlayers, ny)`` -- a zonal flow profile U_j(y), which
+        broadcasts along x as GeophysicalFlows' ``(ny, nlayers)`` form does."""
+        U = np.zeros(self.nlayers) if U is None else np.asarray(U, dtype=np.float64)
+        if U.size == self.nlayers:
+            U = U.reshape(self.nlayers, 1, 1)
+        else:
+            U = U.reshape(self.nlayers, self.grid.ny, 1)
         for j, pr in enumerate(self.layers):
             pr.set_flow_arrays(np.asarray(u[j]) + U[j], np.asarray(v[j]))
 

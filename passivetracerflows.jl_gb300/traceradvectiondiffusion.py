@@ -540,6 +540,23 @@ def _is_multilayer_flow(obj):
         hasattr(obj.params, "nlayers") and hasattr(obj, "grid") and hasattr(obj, "clock")
 
 
+def _layer_mean_flow(U, nl, ny):
+    """``MQGprob.params.U`` split into what ``ptf_set_flow_layers`` takes: one
+    imposed zonal flow per layer (``U_j``), or -- GeophysicalFlows also takes
+    a ``(ny, nlayers)`` matrix -- a profile per layer ``U_j(y)``, returned as
+    an ``(nl, ny, 1)`` array to add to ``u`` (``calcN!`` adds ``params.U``
+    to ``vars.u`` by broadcasting, ``:794``).  Returns ``(per_layer, profile)``
+    with one of the two ``None``."""
+    U = np.asarray(0.0 if U is None else U, dtype=np.float64)
+    if U.size == 1:
+        return np.full(nl, float(U.reshape(-1)[0])), None
+    if U.size == nl:
+        return U.reshape(nl), None
+    if U.size == nl * ny:
+        return None, U.reshape(nl, ny, 1)
+    raise ValueError(f"params.U has {U.size} values: expected 1, nlayers ({nl}) or nlayers x ny ({nl * ny})")
+
+
 class MultiLayerQGFlow:
     """What the tracer needs of a ``GeophysicalFlows.MultiLayerQG`` problem:
     ``grid`` (nx, Lx, ny, Ly), ``params.nlayers``, ``params.U`` (each layer's
@@ -552,7 +569,8 @@ class MultiLayerQGFlow:
     class _Params:
         def __init__(self, nlayers, U):
             self.nlayers = int(nlayers)
-            self.U = np.zeros(self.nlayers) if U is None else np.asarray(U, dtype=np.float64).reshape(self.nlayers)
+            # one value per layer, or (nlayers, ny): a profile U_j(y) per layer
+            self.U = np.zeros(self.nlayers) if U is None else np.asarray(U, dtype=np.float64)
 
     class _Vars:
         def __init__(self, u, v):
@@ -612,12 +630,21 @@ class MultiLayerTracerProblem(Problem):
     def _refresh_flow(self):
         """``u = MQGprob.vars.u + MQGprob.params.U``, ``v = MQGprob.vars.v`` (``:794-795``)."""
         mq = self.MQGprob
-        U = np.asarray(getattr(mq.params, "U", np.zeros(self.nlayers)), dtype=np.float64).reshape(self.nlayers)
+        U, Uy = _layer_mean_flow(getattr(mq.params, "U", None), self.nlayers, self.grid.ny)
         shape = (self.nlayers,) + self.grid.shape
         ptrs, keep = [], []
         on_device = _all_host_or_device((mq.vars.u, mq.vars.v), "MQGprob.vars.u, v")
         where = L.PTF_DEVICE if on_device else L.PTF_HOST
-        for a in (mq.vars.u, mq.vars.v):
+        u = mq.vars.u
+        if Uy is not None:  # a y profile is added to u here; the per-layer constants are then zero
+            if on_device:
+                import torch
+                u = (_device_array(u, math.prod(shape), "MQGprob.vars.u") +
+                     torch.as_tensor(Uy, dtype=torch.float64, device=u.device)).contiguous()
+            else:
+                u = np.broadcast_to(np.asarray(u, dtype=np.float64), shape) + Uy
+            U = np.zeros(self.nlayers)
+        for a in (u, mq.vars.v):
             if on_device:
                 ptrs.append(ct.c_void_p(_device_array(a, math.prod(shape), "MQGprob.vars.u, v").data_ptr()))
                 keep.append(a)

@@ -142,3 +142,41 @@ def test_flow_display(pkg):
     assert s[3] == "  └─ steadyflow: false"
     assert len(str(pkg.ThreeDAdvectingFlow()).splitlines()) == 5
     assert len(str(pkg.OneDAdvectingFlow()).splitlines()) == 3
+
+
+def test_layer_mean_flow_forms(pkg):
+    """MQGprob.params.U: a scalar, one value per layer, or a (nlayers, ny)
+    profile U_j(y) (GeophysicalFlows' (ny, nlayers) matrix) added along x."""
+    from ptf_gb300 import traceradvectiondiffusion as tad
+    per, prof = tad._layer_mean_flow([0.1, -0.2], 2, 8)
+    assert np.allclose(per, [0.1, -0.2]) and prof is None
+    per, prof = tad._layer_mean_flow(0.3, 2, 8)
+    assert np.allclose(per, [0.3, 0.3]) and prof is None
+    Uy = np.arange(16.0).reshape(2, 8)
+    per, prof = tad._layer_mean_flow(Uy, 2, 8)
+    assert per is None and prof.shape == (2, 8, 1) and prof[1, 3, 0] == Uy[1, 3]
+    u = np.zeros((2, 8, 4)) + prof  # broadcasts along x
+    assert np.all(u[1, 3] == Uy[1, 3])
+    with pytest.raises(ValueError):
+        tad._layer_mean_flow(np.zeros(5), 2, 8)
+
+
+def test_oracle_layer_profile_is_u_plus_U_of_y(oracle):
+    """The oracle adds a (nlayers, ny) mean-flow profile to u along x (:794)."""
+    n, nl = 32, 2
+    rng = np.random.default_rng(1)
+    u, v = rng.standard_normal((nl, n, n)) * 0.1, rng.standard_normal((nl, n, n)) * 0.1
+    y = -np.pi + 2 * np.pi / n * np.arange(n)
+    Uy = np.stack([0.5 * np.sin(y), 0.2 * np.cos(2 * y)])
+    a = oracle.MultiLayerProblem(nx=n, nlayers=nl, dt=0.01, kappa=1e-3, stepper="RK4")
+    b = oracle.MultiLayerProblem(nx=n, nlayers=nl, dt=0.01, kappa=1e-3, stepper="RK4")
+    a.set_layer_flows(u, v, Uy)
+    b.set_layer_flows(u + Uy[:, :, None], v, None)
+    x = -np.pi + 2 * np.pi / n * np.arange(n)
+    Y, X = np.meshgrid(y, x, indexing="ij")
+    c0 = np.exp(-(X ** 2 + Y ** 2) / 0.5)
+    for p in (a, b):
+        p.set_c(c0)
+        p.stepforward(5)
+        p.updatevars()
+    assert np.array_equal(a.c, b.c)

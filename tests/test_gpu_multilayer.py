@@ -122,3 +122,27 @@ def test_filtered_steppers(gpu, oracle, dim, stepper):
     assert oracle.rel_l2(p.vars.c, r.vars.c) <= 1e-12
     # the filter removes the top of the spectrum: the Nyquist column is ~tol
     assert np.abs(p.sol[..., -1]).max() <= 1e-10 * np.abs(p.sol).max()
+
+
+def test_multilayer_mean_flow_profile(gpu, oracle):
+    """A y-dependent imposed zonal flow U_j(y) per layer (GeophysicalFlows
+    takes U as a (ny, nlayers) matrix), host and device layer velocities."""
+    torch = pytest.importorskip("torch")
+    nl, n, L, dt = 2, 64, 2 * np.pi, 0.01
+    u, v = layer_fields(nl, n, L, 5)
+    y = -L / 2 + L / n * np.arange(n)
+    Uy = np.stack([0.4 * np.sin(y), -0.3 * np.cos(y)])
+    r = oracle.MultiLayerProblem(nx=n, Lx=L, nlayers=nl, dt=dt, kappa=1e-3, stepper="FilteredRK4")
+    r.set_layer_flows(u, v, Uy)
+    c0 = tracer_ic(nl, n, L)
+    r.set_c(c0)
+    r.stepforward(8)
+    r.updatevars()
+    for dev in (False, True):
+        uu, vv = (torch.from_numpy(u).cuda(), torch.from_numpy(v).cuda()) if dev else (u, v)
+        mq = gpu.MultiLayerQGFlow(nx=n, Lx=L, nlayers=nl, dt=dt, U=Uy, u=uu, v=vv)
+        p = gpu.Problem(mq, κ=1e-3, stepper="FilteredRK4")
+        gpu.set_c(p, c0)
+        gpu.stepforward(p, 8)
+        gpu.updatevars(p)
+        assert oracle.rel_l2(p.vars.c, r.c) <= 1e-12
