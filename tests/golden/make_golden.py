@@ -78,8 +78,25 @@ def abc32_etdrk4():
     return dict(c0=c0, c100=p.vars.c.copy(), t=p.clock.t, step=p.clock.step)
 
 
+def line256():
+    """1D, 256 points, u = 0.4 + 0.2 cos x, κ=1e-3, a Gaussian σ=0.3 plus a
+    cos 3x ripple; RK4 and ETDRK4, dt=0.005, c at step 400 (t = 2)."""
+    out = {}
+    for stepper in ("RK4", "ETDRK4"):
+        p = o.Problem(o.OneDAdvectingFlow(u=lambda x: 0.4 + 0.2 * np.cos(x)), nx=256, Lx=2 * np.pi, kappa=1e-3,
+                      dt=0.005, stepper=stepper)
+        (x,) = p.grid.gridpoints()
+        c0 = np.exp(-x ** 2 / (2 * 0.3 ** 2)) + 0.1 * np.cos(3 * x)
+        o.set_c(p, c0)
+        o.stepforward(p, 400); o.updatevars(p)
+        out["c0"] = c0
+        out[f"c400_{stepper}"] = p.vars.c.copy()
+        out["t"], out["step"] = p.clock.t, p.clock.step
+    return out
+
+
 FIXTURES = {"cellular128_rk4": cellular128_rk4, "cellular128_etdrk4": cellular128_etdrk4,
-            "abc32_etdrk4": abc32_etdrk4}
+            "abc32_etdrk4": abc32_etdrk4, "line256": line256}
 
 if __name__ == "__main__":
     names = sys.argv[1:] or list(FIXTURES)

@@ -41,3 +41,13 @@ def test_golden_abc32_etdrk4(oracle):
     assert oracle.rel_l2(d["c100"], g["c100"]) <= 1e-13
     m0, m1 = g["c0"].sum(), g["c100"].sum()
     assert abs(m1 - m0) / abs(m0) < 1e-10
+
+
+def test_golden_line256(oracle):
+    g = np.load(GOLD / "line256.npz")
+    d = _mod().line256()
+    for k in ("c400_RK4", "c400_ETDRK4"):
+        assert oracle.rel_l2(d[k], g[k]) <= 1e-13, k
+    assert int(g["step"]) == 400
+    # RK4 and ETDRK4 agree to their O(dt^4) difference
+    assert oracle.rel_l2(g["c400_RK4"], g["c400_ETDRK4"]) <= 1e-9

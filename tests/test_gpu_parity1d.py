@@ -120,3 +120,18 @@ def test_1d_autotune_keeps_state(gpu, oracle):
     t = p.autotune(trial_steps=2, force=True)
     assert t["branches"] == 1 and t["ms_per_step"] > 0
     assert np.array_equal(p.sol, before)
+
+
+@pytest.mark.parametrize("stepper", ["RK4", "ETDRK4"])
+def test_golden_line256_400_steps(gpu, stepper):
+    """400 FP64 steps of the 1D golden workload against the committed fixture."""
+    from pathlib import Path
+    g = np.load(Path(__file__).resolve().parent / "golden" / "line256.npz")
+    p = gpu.Problem(gpu.GPU(), gpu.OneDAdvectingFlow(u=lambda x: 0.4 + 0.2 * np.cos(x)), nx=256, κ=1e-3, dt=0.005,
+                    stepper=stepper)
+    gpu.set_c(p, g["c0"])
+    gpu.stepforward(p, 400)
+    gpu.updatevars(p)
+    c = g[f"c400_{stepper}"]
+    assert np.linalg.norm(p.vars.c - c) / np.linalg.norm(c) <= 1e-10
+    assert p.clock.step == 400
