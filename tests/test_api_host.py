@@ -180,3 +180,21 @@ def test_oracle_layer_profile_is_u_plus_U_of_y(oracle):
         p.stepforward(5)
         p.updatevars()
     assert np.array_equal(a.c, b.c)
+
+
+def test_solve_spec_maps_to_the_c_descriptor(pkg):
+    """SolveSpec -> ptf_solve_desc (no device needed): η defaults to κ, the
+    flow and time-mode names map to the ABI's enums."""
+    from ptf_gb300 import _lib as L
+    d = pkg.SolveSpec(n=256, nsteps=40, dt=0.003, kappa=2e-3, flow="cellular", time_mode="stage", U=0.5, eps=0.3,
+                      omega=2.0, Kx=2, Ky=3).desc()
+    assert (d.dim, d.n, d.nsteps) == (2, 256, 40) and d.dt == 0.003
+    assert d.kappa == 2e-3 and d.eta == 2e-3
+    assert d.flow_kind == L.PTF_FLOW_CELLULAR and d.time_mode == L.PTF_STAGE_T
+    assert (d.U, d.eps, d.omega, d.Kx, d.Ky) == (0.5, 0.3, 2.0, 2, 3)
+    assert abs(d.L - 2 * np.pi) < 1e-15
+    d = pkg.SolveSpec(n=64, nsteps=1, dt=0.01, kappa=1e-3, eta=5e-4).desc()
+    assert d.eta == 5e-4 and d.flow_kind == L.PTF_FLOW_ARRAYS and d.time_mode == L.PTF_CLOCK_T
+    assert pkg.SolveSpec(n=32, nsteps=1, dt=0.1, dim=3).points == 32 ** 3
+    with pytest.raises(KeyError):
+        pkg.SolveSpec(n=64, nsteps=1, dt=0.01, flow="turbulent").desc()
