@@ -97,3 +97,38 @@ def test_null_handle_calls_fail_cleanly(pkg):
     assert lib.ptf_set_c(None, None, 0) == L.PTF_ERR_ARG
     assert lib.ptf_synchronize(None) == L.PTF_ERR_ARG
     lib.ptf_destroy(None)
+
+
+@pytest.mark.parametrize("field,value", [("precision", 7), ("memory_budget", -1), ("slots_per_bucket", -2),
+                                         ("max_slots", 0)])
+def test_batch_create_rejects_bad_config(pkg, field, value):
+    from ptf_gb300 import _lib as L
+    lib = L.load()
+    c = L.PtfBatchConfig()
+    lib.ptf_batch_config_default(ct.byref(c))
+    setattr(c, field, value)
+    b = ct.c_void_p()
+    assert lib.ptf_batch_create(ct.byref(c), ct.byref(b)) == L.PTF_ERR_ARG
+    assert not b.value and lib.ptf_batch_last_error(None)
+
+
+@pytest.mark.parametrize("field,value", [("chunk_steps", -1), ("memory_budget", -5), ("precision", 3)])
+def test_server_create_rejects_bad_config(pkg, field, value):
+    from ptf_gb300 import _lib as L
+    lib = L.load()
+    c = L.PtfServerConfig()
+    lib.ptf_server_config_default(ct.byref(c))
+    setattr(c, field, value)
+    s = ct.c_void_p()
+    assert lib.ptf_server_create(ct.byref(c), ct.byref(s)) == L.PTF_ERR_ARG
+    assert not s.value
+
+
+def test_batch_and_server_null_calls_fail_cleanly(pkg):
+    from ptf_gb300 import _lib as L
+    lib = L.load()
+    assert lib.ptf_batch_step(None, 1) == L.PTF_ERR_ARG
+    assert lib.ptf_batch_synchronize(None) == L.PTF_ERR_ARG
+    assert lib.ptf_server_wait_all(None, 0.1) == L.PTF_ERR_ARG
+    lib.ptf_batch_destroy(None)
+    lib.ptf_server_destroy(None)
