@@ -132,3 +132,16 @@ def test_batch_and_server_null_calls_fail_cleanly(pkg):
     assert lib.ptf_server_wait_all(None, 0.1) == L.PTF_ERR_ARG
     lib.ptf_batch_destroy(None)
     lib.ptf_server_destroy(None)
+
+
+def test_noalloc_rejects_bad_arguments_before_the_device(pkg):
+    """ptf_calcN2d_noalloc checks sizes, lengths, pointers and the fixed
+    scratch's capacity before any CUDA call (the pointers are never read)."""
+    from ptf_gb300 import _lib as L
+    lib = L.load()
+    fake = ct.c_void_p(16)  # never dereferenced: every case fails before the device
+    cases = [((100, 64, 1.0, 1.0, fake), L.PTF_ERR_ARG), ((64, 64, -1.0, 1.0, fake), L.PTF_ERR_ARG),
+             ((64, 64, 1.0, 1.0, None), L.PTF_ERR_ARG), ((1024, 1024, 1.0, 1.0, fake), L.PTF_ERR_MEMORY)]
+    for (nx, ny, Lx, Ly, p), want in cases:
+        assert lib.ptf_calcN2d_noalloc(nx, ny, Lx, Ly, p, fake, fake, fake, None) == want
+    assert "1024x1024 does not" in lib.ptf_last_error(None).decode()
