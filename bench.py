@@ -703,9 +703,9 @@ def random_phase_flow(n, rng, dim=2, kmin=4, kmax=16, L=2 * np.pi):
     amp = np.where(mask, np.maximum(K, 1) ** -4.0, 0.0)
     Ah = [amp * np.exp(2j * np.pi * rng.random(K.shape)) for _ in range(3)]
     s = (n, n, n)
-    u = np.fft.irfftn(1j * (l * Ah[2] - m * Ah[1]), s=s)
-    v = np.fft.irfftn(1j * (m * Ah[0] - k * Ah[2]), s=s)
-    w = np.fft.irfftn(1j * (k * Ah[1] - l * Ah[0]), s=s)
+    u = np.fft.irfftn(1j * (l * Ah[2] - m * Ah[1]), s=s, axes=(0, 1, 2))
+    v = np.fft.irfftn(1j * (m * Ah[0] - k * Ah[2]), s=s, axes=(0, 1, 2))
+    w = np.fft.irfftn(1j * (k * Ah[1] - l * Ah[0]), s=s, axes=(0, 1, 2))
     rms = np.sqrt(np.mean(u ** 2 + v ** 2 + w ** 2))
     return u / rms, v / rms, w / rms
 

@@ -39,3 +39,42 @@ def test_reference_arm_line():
 
 def test_reference_arm_other_ranks_are_silent():
     assert _run({"WORLD_SIZE": "2", "RANK": "1", "LOCAL_RANK": "1"}, "--n", "64", "--steps", "1") == []
+
+
+def _bench():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("ptf_bench_mod", ROOT / "bench.py")
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m
+
+
+def test_served_stream_flows_follow_the_workload_definition():
+    """The served stream's random-phase flows: incompressible, rms speed 1,
+    energy only in 4 <= |k| <= 16 with |u_k| ~ |k|^-3 (2D streamfunction; 3D
+    curl of a vector potential)."""
+    import numpy as np
+    b = _bench()
+    rng = np.random.default_rng(0)
+    n = 64
+    u, v = b.random_phase_flow(n, rng)
+    assert abs(np.sqrt(np.mean(u ** 2 + v ** 2)) - 1) < 1e-12
+    uh, vh = np.fft.rfft2(u), np.fft.rfft2(v)
+    l = np.fft.fftfreq(n, 1.0 / n)[:, None]
+    k = np.arange(n // 2 + 1)[None, :]
+    div = k * uh + l * vh
+    assert np.abs(div).max() <= 1e-10 * np.abs(uh).max()
+    K = np.sqrt(k ** 2 + l ** 2)
+    e = np.abs(uh) ** 2 + np.abs(vh) ** 2
+    assert e[(K < 4) | (K > 16)].max() <= 1e-20 * e.max()
+    # |u_k| |k|^3 is the same for every mode of the band (random phases only)
+    band = (K >= 4) & (K <= 16) & (k > 0) & (k < n // 2)
+    r = np.sqrt(e[band]) * K[band] ** 3
+    assert r.max() / r.min() < 1 + 1e-9
+    u3, v3, w3 = b.random_phase_flow(32, rng, dim=3)
+    assert abs(np.sqrt(np.mean(u3 ** 2 + v3 ** 2 + w3 ** 2)) - 1) < 1e-12
+    m3 = np.fft.fftfreq(32, 1.0 / 32)[:, None, None]
+    l3 = np.fft.fftfreq(32, 1.0 / 32)[None, :, None]
+    k3 = np.arange(17)[None, None, :]
+    div3 = k3 * np.fft.rfftn(u3) + l3 * np.fft.rfftn(v3) + m3 * np.fft.rfftn(w3)
+    assert np.abs(div3).max() <= 1e-10 * np.abs(np.fft.rfftn(u3)).max()
