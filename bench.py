@@ -154,11 +154,18 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        rows = [ln.split(",") for ln in Path(self.path).read_text().splitlines() if ln.strip()]
+        lines = Path(self.path).read_text().splitlines()
         os.unlink(self.path)
+        return self.summarize(lines)
+
+    @staticmethod
+    def summarize(lines):
+        """Median SM clock, the maximum clock and every throttle reason seen
+        Active, from `FIELDS` rows (csv, noheader, nounits)."""
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in rows:
+        for ln in lines:
+            r = ln.split(",")
             try:
                 sm.append(float(r[1])); smax = float(r[2])
                 for nm, val in zip(names, r[5:9]):

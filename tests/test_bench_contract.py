@@ -78,3 +78,17 @@ def test_served_stream_flows_follow_the_workload_definition():
     k3 = np.arange(17)[None, None, :]
     div3 = k3 * np.fft.rfftn(u3) + l3 * np.fft.rfftn(v3) + m3 * np.fft.rfftn(w3)
     assert np.abs(div3).max() <= 1e-10 * np.abs(np.fft.rfftn(u3)).max()
+
+
+def test_clock_summary_reports_throttle_reasons():
+    """The `clocks` object: median SM clock under load and every throttle
+    reason seen Active (a run with a slowdown reason is re-measured)."""
+    b = _bench()
+    rows = ["0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active",
+            "0, 2055, 2070, 1350.0, 0x4, Not Active, Not Active, Not Active, Active",
+            "0, 1900, 2070, 1400.0, 0x8, Active, Not Active, Not Active, Active",
+            "", "0, [N/A], 2070, 0, 0x0, , , , "]
+    c = b.ClockSampler.summarize(rows)
+    assert c["samples"] == 3 and c["sm_mhz"] == 2055.0 and c["sm_max_mhz"] == 2070.0
+    assert c["reasons"] == ["hw_slowdown", "sw_power_cap"]
+    assert b.ClockSampler.summarize([]) == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
