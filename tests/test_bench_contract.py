@@ -92,3 +92,16 @@ def test_clock_summary_reports_throttle_reasons():
     assert c["samples"] == 3 and c["sm_mhz"] == 2055.0 and c["sm_max_mhz"] == 2070.0
     assert c["reasons"] == ["hw_slowdown", "sw_power_cap"]
     assert b.ClockSampler.summarize([]) == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+
+
+def test_roofline_traffic_comes_from_the_committed_profile():
+    """`roofline.traffic` of the default run is the ncu DRAM bytes per launch
+    recorded in profiles/, for the dominant pass of that workload."""
+    b = _bench()
+    col, src = b.profiled_traffic("column_pass", "f32", 1024, 16)
+    row, _ = b.profiled_traffic("row_pass", "f32", 1024, 16)
+    assert src == "pass2d_fp32_1024x1024_b16_etdrk4.md"
+    assert col == 351896576 and row == 184454208
+    assert b.profiled_traffic("column_pass", "f32", 2048, 16) == (None, None)
+    peak, kind = b.load_peaks()
+    assert peak > 1000 and kind in ("measured", "fallback")
