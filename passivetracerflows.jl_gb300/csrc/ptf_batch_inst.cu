@@ -1,5 +1,6 @@
-// Explicit instantiation of one persistent batched stage kernel:
-// -DPTF_T=float|double -DPTF_MODE=<RK4 stage ColMode 2..5>.
+// Explicit instantiation of the batched stage kernels for one precision and
+// one RK4 stage (the per-item row and column launches and the persistent
+// form): -DPTF_T=float|double -DPTF_MODE=<RK4 stage ColMode 2..5>.
 #include "ptf_batch_kern.cuh"
 
 #if !defined(PTF_T) || !defined(PTF_MODE)

@@ -1,4 +1,5 @@
-// Persistent per-stage kernel of the batched form and its work plan.  See
+// Stage kernels of the batched form (per-item row and column launches, and
+// the persistent per-stage kernel) and their work plan.  See
 // ptf_batch.cu for the design; the kernels are instantiated per (precision,
 // stage) in ptf_batch_inst.cu so they compile in parallel.
 #pragma once

@@ -1,7 +1,7 @@
 // Request server: continuous batching of tracer solves on one GPU.
 //
 // A worker thread owns a ptf_batch (square 2D solves, stepped together by
-// the persistent batched kernels) and a set of single-solve handles (3D
+// the batched stage kernels) and a set of single-solve handles (3D
 // requests).  Each loop iteration it (1) admits queued requests in arrival
 // order wherever the device-memory budget and the bucket slots allow,
 // (2) advances every admitted solve by one chunk of steps -- the chunk ends
