@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define PTF_ABI_VERSION 2
+#define PTF_ABI_VERSION 3
 
 enum ptf_status {
   PTF_OK = 0,
@@ -239,6 +239,10 @@ typedef struct ptf_batch_config {
   int32_t persistent;       /* 1: one persistent kernel per stage (items from an atomic counter, a
                                bounded wait between a bucket's row and column items); 0 (default):
                                a row launch and a column launch per stage, one block per item */
+  int32_t k0_mode;          /* FP32 only: 1 (default) carries each solve's conserved (0,0) mode in
+                               FP64 (seeded from a compensated sum of c0, stage combinations in
+                               FP64, N(0,0) a compensated FP64 sum; readback shifted so that the
+                               field's sum is that mode), as ptf_config.k0_mode; 0: all FP32 */
 } ptf_batch_config;
 
 typedef struct ptf_batch ptf_batch;
@@ -283,6 +287,9 @@ typedef struct ptf_server_stats {
   double grid_point_steps;      /* sum over completed requests of points x steps */
   double wall_s;                /* first submission to last completion */
   int64_t device_bytes;
+  double mass_drift_max_abs;    /* max over completed requests of |sum(c_end) / sum(c0) - 1| */
+  int64_t batch_solves;         /* solves holding a slot of the batched form (2D) */
+  int64_t handles;              /* single-solve handles alive (3D) */
 } ptf_server_stats;
 
 typedef struct ptf_server ptf_server;
@@ -292,7 +299,11 @@ void ptf_server_config_default(ptf_server_config* cfg);
 int ptf_server_create(const ptf_server_config* cfg, ptf_server** out);
 void ptf_server_destroy(ptf_server* s);
 const char* ptf_server_last_error(const ptf_server* s);
-/* Copies the inputs; w only for 3D.  Returns immediately. */
+/* Copies the inputs; w only for 3D.  Returns immediately.  A request that
+ * could not be admitted even into an empty server under its memory budget
+ * is refused here with PTF_ERR_MEMORY (as the reference refuses invalid
+ * Problem arguments at construction, src/traceradvectiondiffusion.jl:234),
+ * instead of queueing for ever. */
 int ptf_server_submit(ptf_server* s, const ptf_solve_desc* d, const double* c0, const double* u, const double* v,
                       const double* w, int64_t* id);
 /* state: ptf_request_state; copies the tracer field into c when done. */
@@ -300,6 +311,17 @@ int ptf_server_poll(ptf_server* s, int64_t id, int32_t* state, double* c);
 int ptf_server_release(ptf_server* s, int64_t id);
 int ptf_server_wait_all(ptf_server* s, double timeout_s);
 int ptf_server_get_stats(ptf_server* s, ptf_server_stats* out);
+/* Per-request result record (no reference counterpart): latency from
+ * submission to result, and the tracer mass (sum of c, compensated FP64)
+ * of the initial condition and of the result -- the mass drift of every
+ * result is mass_end / mass0 - 1.  The request must be done. */
+int ptf_server_result_info(ptf_server* s, int64_t id, double* latency_s, double* mass0, double* mass_end);
+/* Host-side fault injection for tests (no reference counterpart): the chunk
+ * of steps `chunks_from_now` chunks after the next one (0: the next) reports
+ * a step failure as if the batched step had returned PTF_ERR_CUDA.  Nothing
+ * is faulted on the GPU; the server fails the requests in flight, releases
+ * their slots and handles, and keeps serving.  A negative value cancels. */
+int ptf_server_inject_step_failure(ptf_server* s, int32_t chunks_from_now);
 
 /* Size of the fixed device scratch used by ptf_calcN2d_noalloc (16 MiB). */
 #define PTF_NOALLOC_SCRATCH_BYTES (16u << 20)
@@ -321,7 +343,10 @@ int ptf_server_get_stats(ptf_server* s, ptf_server_stats* out);
  * PTF_ERR_MEMORY.  The first call on a device does a one-time set-up (symbol
  * address lookup and a synchronous twiddle upload); make it before any
  * stream capture.  All calls share that array and it keeps the last call's
- * contents, so calls that overlap on the GPU race.  Errors: ptf_last_error(NULL). */
+ * contents, so calls that overlap on the GPU race.  The set-up is kept per
+ * device for the life of the process: resetting a device (cudaDeviceReset)
+ * after its first call is not supported, since the kept address belongs to
+ * the context the reset destroyed.  Errors: ptf_last_error(NULL). */
 int ptf_calcN2d_noalloc(int32_t nx, int32_t ny, double Lx, double Ly, const double* sol, const double* u,
                         const double* v, double* N, void* stream);
 

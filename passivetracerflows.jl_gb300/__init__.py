@@ -15,8 +15,10 @@ from .traceradvectiondiffusion import (CPU, GPU, Problem, OneDAdvectingFlow, Thr
                                        stepforward, updatevars, MultiLayerQGFlow, MultiLayerTracerProblem)
 from ._lib import LIB_PATH, load as load_library
 from .batched import BatchedProblem, Server, SolveSpec
+from .output import Output, get_concentration, get_sol, jldopen, saveoutput, saveproblem
 
 __all__ = ["TracerAdvectionDiffusion", "CPU", "GPU", "Problem", "OneDAdvectingFlow", "TwoDAdvectingFlow",
            "ThreeDAdvectingFlow", "OneDGrid", "TwoDGrid", "ThreeDGrid", "gridpoints", "noflow", "set_c", "stepforward",
            "updatevars", "LIB_PATH", "load_library", "BatchedProblem", "Server", "SolveSpec", "MultiLayerQGFlow",
-           "MultiLayerTracerProblem"]
+           "MultiLayerTracerProblem", "Output", "saveproblem", "saveoutput", "jldopen", "get_sol",
+           "get_concentration"]

@@ -52,7 +52,8 @@ class PtfSolveDesc(ct.Structure):
 
 class PtfBatchConfig(ct.Structure):
     _fields_ = [("precision", ct.c_int32), ("memory_budget", ct.c_int64), ("slots_per_bucket", ct.c_int32),
-                ("use_graph", ct.c_int32), ("max_slots", ct.c_int32), ("persistent", ct.c_int32)]
+                ("use_graph", ct.c_int32), ("max_slots", ct.c_int32), ("persistent", ct.c_int32),
+                ("k0_mode", ct.c_int32)]
 
 
 class PtfServerConfig(ct.Structure):
@@ -63,7 +64,8 @@ class PtfServerConfig(ct.Structure):
 class PtfServerStats(ct.Structure):
     _fields_ = [("completed", ct.c_int64), ("failed", ct.c_int64), ("queued", ct.c_int64), ("active", ct.c_int64),
                 ("p50_s", ct.c_double), ("p99_s", ct.c_double), ("mean_s", ct.c_double),
-                ("grid_point_steps", ct.c_double), ("wall_s", ct.c_double), ("device_bytes", ct.c_int64)]
+                ("grid_point_steps", ct.c_double), ("wall_s", ct.c_double), ("device_bytes", ct.c_int64),
+                ("mass_drift_max_abs", ct.c_double), ("batch_solves", ct.c_int64), ("handles", ct.c_int64)]
 
 
 class PtfTuning(ct.Structure):
@@ -137,6 +139,9 @@ SIGNATURES = {
     "ptf_server_release": (ct.c_int, [ct.c_void_p, ct.c_int64]),
     "ptf_server_wait_all": (ct.c_int, [ct.c_void_p, ct.c_double]),
     "ptf_server_get_stats": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfServerStats)]),
+    "ptf_server_result_info": (ct.c_int, [ct.c_void_p, ct.c_int64, ct.POINTER(ct.c_double), ct.POINTER(ct.c_double),
+                                          ct.POINTER(ct.c_double)]),
+    "ptf_server_inject_step_failure": (ct.c_int, [ct.c_void_p, ct.c_int32]),
     "ptf_set_schedule": (ct.c_int, [ct.c_void_p, ct.c_int32, ct.c_int32, ct.c_int32]),
     "ptf_set_flow_layers": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int32]),
     "ptf_set_flow_analytic": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfFlowDesc)]),

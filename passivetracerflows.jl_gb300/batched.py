@@ -77,7 +77,7 @@ class BatchedProblem:
     with ``persistent=True`` -- steps replayed from a captured CUDA graph)."""
 
     def __init__(self, T=np.float32, memory_budget=0, slots_per_bucket=0, use_graph=True, max_slots=4096,
-                 persistent=False):
+                 persistent=False, k0_mode=True):
         lib = L.load()
         cfg = L.PtfBatchConfig()
         lib.ptf_batch_config_default(ct.byref(cfg))
@@ -87,6 +87,7 @@ class BatchedProblem:
         cfg.use_graph = 1 if use_graph else 0
         cfg.max_slots = int(max_slots)
         cfg.persistent = 1 if persistent else 0
+        cfg.k0_mode = 1 if k0_mode else 0
         h = ct.c_void_p()
         L.check(lib.ptf_batch_create(ct.byref(cfg), ct.byref(h)), None)
         self._h = h
@@ -201,3 +202,17 @@ class Server:
         s = L.PtfServerStats()
         self._check(L.load().ptf_server_get_stats(self._h, ct.byref(s)))
         return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def result_info(self, rid):
+        """Latency (s) and tracer mass (sum of c, compensated FP64) of the initial
+        condition and of the result of a finished request; its mass drift is
+        ``mass_end / mass0 - 1``."""
+        lat, m0, m1 = ct.c_double(), ct.c_double(), ct.c_double()
+        self._check(L.load().ptf_server_result_info(self._h, rid, ct.byref(lat), ct.byref(m0), ct.byref(m1)))
+        return {"latency_s": lat.value, "mass0": m0.value, "mass_end": m1.value,
+                "mass_drift": (m1.value / m0.value - 1.0) if m0.value else float("nan")}
+
+    def inject_step_failure(self, chunks_from_now=0):
+        """Test hook: the chunk of steps that many chunks after the next one
+        reports a step failure (host-side; nothing is faulted on the GPU)."""
+        self._check(L.load().ptf_server_inject_step_failure(self._h, int(chunks_from_now)))

@@ -77,7 +77,11 @@ struct Bucket {
   int slot_base = 0;               // first entry of the bucket in the slot parameter array
   std::vector<long long> owner;    // solve id per slot, -1 when free
   int W = 1, P = 1;                // single-slot launch shapes (admission, readback)
-  size_t bytes = 0;
+  size_t bytes = 0;                // device bytes of the bucket's fields
+  std::vector<void*> allocs;       // the bucket's own device allocations
+  size_t alloc_bytes = 0;          // their total
+  bool dead = false;               // released (its slot range stays reserved for a new bucket)
+  int span = 0;                    // slots of the parameter table reserved for this entry (>= cap)
 };
 
 struct SolveRef {
@@ -100,6 +104,11 @@ struct ptf_batch {
   std::vector<unsigned char> slots_host;
   void* slot_list_dev = nullptr;  // per-bucket active-slot lists, concatenated
   void* plan_dev = nullptr;
+  // FP64 k = 0 mode (FP32 batches): per slot {s, stage input, acc, L(0,0)},
+  // then 64 sum partials and one sum for readback
+  bool k0mode = false;
+  double* k0 = nullptr;
+  double k0_seed[3] = {0, 0, 0};  // host source of the seed copy (kept alive until it completes)
   unsigned int* ctr = nullptr;
   int* err = nullptr;
   double* stage = nullptr;
@@ -107,6 +116,7 @@ struct ptf_batch {
   std::map<long long, SolveRef> solves;
   long long next_id = 1;
   bool plan_dirty = true;
+  long long bucket_gen = 0, plan_gen = -1;  // bumped when a bucket's buffers change
   int plan_total = 0, plan_row_total = 0;
   std::vector<int> plan_lists;      // active slots per bucket of the current plan
   std::vector<int> plan_buckets;
@@ -136,6 +146,38 @@ bool balloc(ptf_batch* b, void** p, size_t bytes) {
   b->allocs.push_back(*p);
   b->bytes += bytes;
   return cudaMemsetAsync(*p, 0, bytes, b->stream) == cudaSuccess;
+}
+
+bool bucket_alloc(ptf_batch* b, Bucket& k, void** p, size_t bytes) {
+  if (cudaMalloc(p, bytes) != cudaSuccess) { *p = nullptr; cudaGetLastError(); return false; }
+  k.allocs.push_back(*p);
+  k.alloc_bytes += bytes;
+  b->bytes += bytes;
+  return cudaMemsetAsync(*p, 0, bytes, b->stream) == cudaSuccess;
+}
+
+void free_bucket(ptf_batch* b, Bucket& k) {
+  cudaStreamSynchronize(b->stream);
+  for (void* p : k.allocs) cudaFree(p);
+  k.allocs.clear();
+  b->bytes -= std::min(b->bytes, k.alloc_bytes);
+  k.alloc_bytes = 0;
+  k.s = k.si = k.acc = k.A = k.B = k.Nx = k.u = k.v = k.phys = k.tw = nullptr;
+  k.dead = true;
+  k.n = 0;
+  b->bucket_gen++;
+  b->plan_dirty = true;
+}
+
+// Under a memory budget, release the buckets that hold no solve (their slot
+// ranges stay reserved and are reused by later buckets that fit in them).
+void reclaim_empty_buckets(ptf_batch* b) {
+  for (Bucket& k : b->buckets) {
+    if (k.dead) continue;
+    bool empty = true;
+    for (long long o : k.owner) if (o >= 0) { empty = false; break; }
+    if (empty) free_bucket(b, k);
+  }
 }
 
 size_t per_slot_bytes(const ptf_batch* b, int n) {
@@ -174,20 +216,39 @@ int new_bucket(ptf_batch* b, int n, double L) {
   int cap = default_cap(b, n);
   const size_t ps = per_slot_bytes(b, n);
   if (b->cfg.memory_budget > 0) {
-    const long long left = b->cfg.memory_budget - (long long)b->bytes;
+    long long left = b->cfg.memory_budget - (long long)b->bytes;
+    if (left < (long long)ps) {  // empty buckets of other sizes may hold the room
+      reclaim_empty_buckets(b);
+      left = b->cfg.memory_budget - (long long)b->bytes;
+    }
     const long long fit = left > 0 ? left / (long long)ps : 0;
     if (fit < 1) return -1;
     cap = (int)std::min<long long>(cap, fit);
   }
-  if ((int)b->buckets.size() >= kMaxBuckets) return -1;
-  if (b->slot_used + cap > b->slot_cap) cap = b->slot_cap - b->slot_used;
+  // a released entry whose slot range is large enough, else a new entry
+  int reuse = -1;
+  for (size_t i = 0; i < b->buckets.size(); ++i)
+    if (b->buckets[i].dead && b->buckets[i].span >= 1 && (reuse < 0 || b->buckets[i].span > b->buckets[reuse].span))
+      reuse = (int)i;
+  if (reuse >= 0) {
+    cap = std::min(cap, b->buckets[reuse].span);
+  } else {
+    if ((int)b->buckets.size() >= kMaxBuckets) return -1;
+    if (b->slot_used + cap > b->slot_cap) cap = b->slot_cap - b->slot_used;
+  }
   if (cap < 1) return -1;
   k.cap = cap;
   const size_t sc = (size_t)cap * n * k.pitch * ec(b), sp = (size_t)cap * n * n * er(b);
-  bool ok = balloc(b, &k.s, sc) && balloc(b, &k.si, sc) && balloc(b, &k.acc, sc) && balloc(b, &k.A, sc) &&
-            balloc(b, &k.B, sc) && balloc(b, &k.Nx, sc) && balloc(b, &k.u, sp) && balloc(b, &k.v, sp) &&
-            balloc(b, &k.phys, sp) && balloc(b, &k.tw, (size_t)n * ec(b));
-  if (!ok) return -2;
+  bool ok = bucket_alloc(b, k, &k.s, sc) && bucket_alloc(b, k, &k.si, sc) && bucket_alloc(b, k, &k.acc, sc) &&
+            bucket_alloc(b, k, &k.A, sc) && bucket_alloc(b, k, &k.B, sc) && bucket_alloc(b, k, &k.Nx, sc) &&
+            bucket_alloc(b, k, &k.u, sp) && bucket_alloc(b, k, &k.v, sp) && bucket_alloc(b, k, &k.phys, sp) &&
+            bucket_alloc(b, k, &k.tw, (size_t)n * ec(b));
+  if (!ok) {
+    cudaStreamSynchronize(b->stream);
+    for (void* p : k.allocs) cudaFree(p);
+    b->bytes -= std::min(b->bytes, k.alloc_bytes);
+    return -2;
+  }
   std::vector<double> tw;
   host_twiddles_d(tw, n);
   cudaError_t e;
@@ -199,15 +260,29 @@ int new_bucket(ptf_batch* b, int n, double L) {
     e = cudaMemcpyAsync(k.tw, tw.data(), tw.size() * sizeof(double), cudaMemcpyHostToDevice, b->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   }
-  if (e != cudaSuccess) return -2;
-  k.slot_base = b->slot_used;
-  b->slot_used += cap;
+  if (e != cudaSuccess) {
+    cudaStreamSynchronize(b->stream);
+    for (void* p : k.allocs) cudaFree(p);
+    b->bytes -= std::min(b->bytes, k.alloc_bytes);
+    return -2;
+  }
   k.owner.assign(cap, -1);
   k.bytes = ps * cap;
   k.W = b->fp32 ? default_lines_per_block<float>(n, true, k.pitch) : default_lines_per_block<double>(n, true, k.pitch);
   k.P = b->fp32 ? default_lines_per_block<float>(n, false, n / 2) : default_lines_per_block<double>(n, false, n / 2);
-  b->buckets.push_back(k);
+  b->bucket_gen++;
   b->plan_dirty = true;
+  if (reuse >= 0) {
+    Bucket& old = b->buckets[reuse];
+    k.slot_base = old.slot_base;
+    k.span = old.span;  // slots of the range beyond the new capacity stay inactive
+    old = k;
+    return reuse;
+  }
+  k.slot_base = b->slot_used;
+  k.span = cap;
+  b->slot_used += cap;
+  b->buckets.push_back(k);
   return (int)b->buckets.size() - 1;
 }
 
@@ -265,6 +340,20 @@ template <typename T> int admit(ptf_batch* b, Bucket& k, int slot, const ptf_sol
   cudaError_t e = cudaMemcpyAsync(b->stage, c0, np * sizeof(double), cudaMemcpyHostToDevice, b->stream);
   if (e == cudaSuccess) e = launch_real_in<T>(b->stage, (T*)k.phys + poff, np, 1.0, b->stream);
   if (e != cudaSuccess) return bcuda(b, e, "admission copy");
+  if (b->k0mode) {
+    // the slot's (0,0) mode in FP64: s = sum of c0 (compensated, from the FP64
+    // input), stage input and accumulator 0, and L(0,0) (non-zero only for
+    // hyperdiffusion of order 0, which damps every mode alike)
+    double* q = b->k0 + 4 * (size_t)(k.slot_base + slot);
+    e = launch_solve_sums<double>(b->stage, np, 1, b->k0 + 4 * (size_t)b->slot_cap, q, 4, b->stream);
+    b->k0_seed[0] = 0.0;
+    b->k0_seed[1] = 0.0;
+    b->k0_seed[2] = d.nkappah == 0 ? -d.kappah : 0.0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(q + 1, b->k0_seed, 3 * sizeof(double), cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return bcuda(b, e, "k = 0 mode seed");
+    b->launches += 2;
+  }
   RowArgs<T> r = slot_row<T>(b, k, slot, ROW_R2C);
   r.scale = (T)0.5;
   e = launch_row<T>(k.n, r, k.P, (k.n / 2) / k.P, 1, b->stream);
@@ -332,6 +421,7 @@ template <typename T> int build_plan(ptf_batch* b) {
     c.stride = k.pitch; c.do_inverse = 1;
     c.bstride = (long long)k.n * k.pitch; c.tplane = c.bstride;
     c.slots = (const SlotParams<T>*)b->slots_dev + k.slot_base;
+    c.k0 = b->k0mode ? b->k0 + 4 * (size_t)k.slot_base : nullptr;
     c.nslots = (int)act.size();
     c.slot_cols = k.pitch;
     RowArgs<T>& r = bp.row;
@@ -361,12 +451,13 @@ template <typename T> int build_plan(ptf_batch* b) {
   }
   std::vector<int> pbk;
   for (size_t bi = 0; bi < b->buckets.size(); ++bi) pbk.push_back(b->buckets[bi].cap);
-  if (b->gexec && lists == b->plan_lists && pbk == b->plan_buckets) {
+  if (b->gexec && lists == b->plan_lists && pbk == b->plan_buckets && b->plan_gen == b->bucket_gen) {
     b->plan_dirty = false;  // same active set: keep the plan and the captured step
     return PTF_OK;
   }
   b->plan_lists = lists;
   b->plan_buckets = pbk;
+  b->plan_gen = b->bucket_gen;
   plan.nb = nb;
   int off = 0;
   for (int i = 0; i < nb; ++i) { plan.b[i].row_begin = off; off += plan.b[i].row_items; }
@@ -500,7 +591,17 @@ template <typename T> int get_c_impl(ptf_batch* b, const Bucket& k, int slot, do
   RowArgs<T> r = slot_row<T>(b, k, slot, ROW_C2R);
   r.scale = (T)(1.0 / (double)np);
   cudaError_t e = launch_row<T>(k.n, r, k.P, (k.n / 2) / k.P, 1, b->stream);
-  if (e == cudaSuccess) e = launch_real_out<T>((const T*)k.phys + (size_t)slot * np, b->stage, np, b->stream);
+  const T* phys = (const T*)k.phys + (size_t)slot * np;
+  if (b->k0mode) {
+    // shift the field so that its sum is the slot's FP64 (0,0) mode
+    double* part = b->k0 + 4 * (size_t)b->slot_cap;
+    if (e == cudaSuccess) e = launch_solve_sums<T>(phys, np, 1, part, part + 64, 1, b->stream);
+    if (e == cudaSuccess)
+      e = launch_real_out_shift<T>(phys, b->stage, np, 1, b->k0 + 4 * (size_t)(k.slot_base + slot), part + 64, b->stream);
+    b->launches += 2;
+  } else if (e == cudaSuccess) {
+    e = launch_real_out<T>(phys, b->stage, np, b->stream);
+  }
   if (e == cudaSuccess) e = cudaMemcpyAsync(c, b->stage, np * sizeof(double), cudaMemcpyDeviceToHost, b->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   if (e != cudaSuccess) return bcuda(b, e, "batched readback");
@@ -525,6 +626,15 @@ int validate(ptf_batch* b, const ptf_solve_desc* d) {
 
 }  // namespace
 
+int64_t ptf::batch_fixed_bytes(const ptf_batch* b) {
+  int64_t bytes = (int64_t)b->bytes;
+  for (const Bucket& k : b->buckets) bytes -= (int64_t)k.alloc_bytes;
+  return bytes;
+}
+int64_t ptf::batch_slot_bytes(const ptf_batch* b, int n) {
+  return (int64_t)per_slot_bytes(b, n) + (int64_t)n * (int64_t)ec(b);  // fields of one slot + the bucket's twiddles
+}
+
 extern "C" {
 
 void ptf_batch_config_default(ptf_batch_config* c) {
@@ -535,6 +645,7 @@ void ptf_batch_config_default(ptf_batch_config* c) {
   c->slots_per_bucket = 0;
   c->use_graph = 1;
   c->max_slots = 4096;
+  c->k0_mode = 1;
 }
 
 void ptf_solve_desc_default(ptf_solve_desc* d) {
@@ -558,6 +669,7 @@ int ptf_batch_create(const ptf_batch_config* cfg, ptf_batch** out) {
   if (cfg->precision != PTF_FP32 && cfg->precision != PTF_FP64) return bfail(nullptr, PTF_ERR_ARG, "precision must be FP64 or FP32");
   if (cfg->memory_budget < 0 || cfg->slots_per_bucket < 0 || cfg->max_slots < 1)
     return bfail(nullptr, PTF_ERR_ARG, "invalid batch limits");
+  if (cfg->k0_mode != 0 && cfg->k0_mode != 1) return bfail(nullptr, PTF_ERR_ARG, "k0_mode must be 0 or 1");
   ptf_batch* b = new ptf_batch();
   b->cfg = *cfg;
   b->fp32 = cfg->precision == PTF_FP32;
@@ -571,6 +683,8 @@ int ptf_batch_create(const ptf_batch_config* cfg, ptf_batch** out) {
             balloc(b, (void**)&b->err, sizeof(int));
   b->stage_elems = (size_t)1024 * 1024;
   ok = ok && balloc(b, (void**)&b->stage, b->stage_elems * sizeof(double));
+  b->k0mode = b->fp32 && cfg->k0_mode == 1;
+  if (b->k0mode) ok = ok && balloc(b, (void**)&b->k0, (4 * (size_t)b->slot_cap + 65) * sizeof(double));
   if (!ok) { ptf_batch_destroy(b); return bfail(nullptr, PTF_ERR_MEMORY, "batch allocation failed"); }
   const int rc = b->fp32 ? setup_kernels<float>(b) : setup_kernels<double>(b);
   if (rc) { std::string m = b->error; ptf_batch_destroy(b); return bfail(nullptr, rc, m); }
@@ -583,6 +697,8 @@ void ptf_batch_destroy(ptf_batch* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
   if (b->graph) cudaGraphDestroy(b->graph);
+  for (Bucket& k : b->buckets)
+    for (void* p : k.allocs) cudaFree(p);
   for (void* p : b->allocs) cudaFree(p);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
@@ -598,8 +714,16 @@ int ptf_batch_can_admit(ptf_batch* b, const ptf_solve_desc* d) {
       for (long long o : k.owner)
         if (o < 0) return 1;
   const size_t ps = per_slot_bytes(b, d->n);
-  if ((int)b->buckets.size() >= kMaxBuckets || b->slot_used >= b->slot_cap) return 0;
-  if (b->cfg.memory_budget > 0 && (long long)(b->bytes + ps) > b->cfg.memory_budget) return 0;
+  size_t reclaimable = 0;
+  bool dead_entry = false;
+  for (const Bucket& k : b->buckets) {
+    if (k.dead) { dead_entry = true; continue; }
+    bool empty = true;
+    for (long long o : k.owner) if (o >= 0) { empty = false; break; }
+    if (empty) reclaimable += k.alloc_bytes;
+  }
+  if (!dead_entry && ((int)b->buckets.size() >= kMaxBuckets || b->slot_used >= b->slot_cap)) return 0;
+  if (b->cfg.memory_budget > 0 && (long long)(b->bytes - reclaimable + ps) > b->cfg.memory_budget) return 0;
   return 1;
 }
 

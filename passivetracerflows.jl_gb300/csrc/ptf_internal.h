@@ -12,6 +12,12 @@ namespace ptf {
 // Message returned by ptf_last_error(NULL) (calls without a handle).
 void set_global_error(const std::string& msg);
 
+// Device bytes a batch holds besides its buckets (slot table, plan, staging),
+// and the bytes one slot of an n x n solve needs (ptf_batch.cu): the request
+// server refuses a request that could not fit even in an empty batch.
+int64_t batch_fixed_bytes(const ptf_batch* b);
+int64_t batch_slot_bytes(const ptf_batch* b, int n);
+
 // Pass launchers (ptf_kern2d.cu dispatching to ptf_k2d_inst.cu objects).
 // Column pass over transform length n: grid (nbx, nby), W columns per block.
 // carve: preferred shared-memory carve-out in percent (-1: the CUDA driver's choice).

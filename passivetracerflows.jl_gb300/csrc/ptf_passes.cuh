@@ -83,7 +83,9 @@ template <typename T> struct ColArgs {
   int nslots, slot_cols;
   // FP64 k = 0 mode (FP32 handles, main column pass): per-solve FP64 state
   // {s, stage input (ETDRK4: d), acc, -} of the (0,0[,0]) mode and its FP64
-  // coefficients {L, E, E2, zeta, alpha, beta, gamma}; null when off
+  // coefficients {L, E, E2, zeta, alpha, beta, gamma}; null when off.
+  // Batched form: {s, stage input, acc, L(0,0)} per slot of the bucket
+  // (RK4 needs no other coefficient; dt comes from the slot), k0c unused.
   double* k0;
   const double* k0c;
   double dt64;
@@ -187,6 +189,40 @@ __device__ __forceinline__ double column0_sum(const C* v, int w, int t, C* line0
       tot = u;
     }
     for (int off = 16; off > 0; off /= 2) tot += __shfl_xor_sync(0xffffffffu, tot, off);
+  }
+  __syncthreads();
+  return tot;
+}
+
+// The same sum for the batched form, where a block's W lines run over the
+// columns of several slots: every line holding column 0 of its slot (`mine`,
+// uniform along the line) sums its E values per thread, then the line's
+// thread t = 0 (which owns position 0) adds the TPL partials, compensated.
+// Returned in that thread; every thread of the block must call this.
+template <typename T, typename C, int E, int TPL>
+__device__ __forceinline__ double column0_sum_lines(const C* v, int w, int t, bool mine, C* sm) {
+  double* part = reinterpret_cast<double*>(sm);  // W*TPL doubles fit in the W lines
+  if (mine) {
+    double s = 0, c = 0;
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const double y = (double)v[i].x - c;
+      const double u = s + y;
+      c = (u - s) - y;
+      s = u;
+    }
+    part[w * TPL + t] = s;
+  }
+  __syncthreads();
+  double tot = 0;
+  if (mine && t == 0) {
+    double c = 0;
+    for (int k = 0; k < TPL; ++k) {
+      const double y = part[w * TPL + k] - c;
+      const double u = tot + y;
+      c = (u - tot) - y;
+      tot = u;
+    }
   }
   __syncthreads();
   return tot;
@@ -354,6 +390,8 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
 
   constexpr bool K0MODE = (MODE >= COL_RK4_1 && MODE <= COL_ETD_4) || MODE == COL_FWD_STORE;
   const bool k0blk = !BATCHED && K0MODE && a.k0 != nullptr && tile == 0;  // uniform across the block
+  // batched form: a.k0 holds {s, stage input, acc, L(0,0)} per slot of the bucket
+  const bool k0bat = BATCHED && K0MODE && a.k0 != nullptr;  // uniform across the block
   double k0N = 0;
   // the combination's first state operand, fetched into this thread's park
   // slots while the forward transform runs (the slots are free until the
@@ -374,9 +412,11 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
     // the rows, real), taken here as a compensated FP64 sum instead of from
     // the FP32 transform; it lands in thread 0, which owns position 0.
     if (k0blk && MODE != COL_FWD_STORE) k0N = column0_sum<T, C, E, TPL>(v, w, t, sm);
+    if (k0bat && MODE != COL_FWD_STORE) k0N = column0_sum_lines<T, C, E, TPL>(v, w, t, store && col == 0, sm);
     fft_line<N, -1, E>(v, t, line, a.tw);
   }
-  const bool k0thr = k0blk && threadIdx.x == 0;  // column 0, t = 0: position p = 0 is its register 0
+  // column 0, t = 0: position p = 0 is its register 0
+  const bool k0thr = (k0blk && threadIdx.x == 0) || (k0bat && store && col == 0 && t == 0);
 
   // Stage combination at the positions p = reg_pos<N, RF, E>(t, i); the
   // next stage input is parked (each thread reads back only its own slots,
@@ -423,9 +463,16 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
       }
       if (k0thr && i == 0) {
         // the (0,0) mode in FP64: {s, stage input (ETDRK4: d), acc, -} of this solve
-        double* q = a.k0 + (size_t)blk * 4;
+        double* q = a.k0 + (size_t)(BATCHED ? slot : blk) * 4;
         const double* kc = a.k0c;
-        const double dd = a.dt64, Nd = k0N;
+        double dd = a.dt64;
+        double kcs[7] = {0, 0, 0, 0, 0, 0, 0};
+        if (BATCHED) {  // RK4: only L(0,0) enters, kept in the slot's fourth value; FP64 dt from the slot
+          kcs[0] = q[3];
+          kc = kcs;
+          dd = a.slots[slot].dtd;
+        }
+        const double Nd = k0N;
         const double xd = k0_combine<MODE>(q, kc, dd, Nd);
         x.x = (T)xd; x.y = 0;
         if (MODE == COL_FWD_STORE || MODE == COL_RK4_4 || MODE == COL_ETD_4) S[o] = x;

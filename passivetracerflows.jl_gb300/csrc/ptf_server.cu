@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -41,8 +42,20 @@ struct Request {
   int64_t batch_id = -1;        // 2D: id in the batch
   ptf_handle* handle = nullptr; // 3D: its own handle
   int64_t done_steps = 0;
+  double mass0 = 0.0, mass_end = 0.0;  // sum of c0 and of the result (compensated FP64)
   std::string error;
 };
+
+// Compensated (Neumaier) sum of n doubles.
+double mass_of(const double* x, size_t n) {
+  double s = 0.0, c = 0.0;
+  for (size_t i = 0; i < n; ++i) {
+    const double t = s + x[i];
+    c += std::fabs(s) >= std::fabs(x[i]) ? (s - t) + x[i] : (x[i] - t) + s;
+    s = t;
+  }
+  return s + c;
+}
 
 }  // namespace
 
@@ -64,6 +77,8 @@ struct ptf_server {
   bool started = false;
   Clock::time_point t_first, t_last;
   int64_t completed = 0, failed = 0;
+  double mass_drift_max = 0.0;
+  int inject_fail_in = -1;  // host-side fault injection: fail the chunk this many chunks ahead (-1: none)
   std::string error;
 };
 
@@ -110,10 +125,9 @@ bool try_admit(ptf_server* s, int64_t id, Request& q) {
     int64_t bid = -1;
     const double* u = q.desc.flow_kind == PTF_FLOW_ARRAYS ? q.u.data() : nullptr;
     const double* v = q.desc.flow_kind == PTF_FLOW_ARRAYS ? q.v.data() : nullptr;
-    if (ptf_batch_add(s->batch, &q.desc, q.c0.data(), u, v, &bid) != PTF_OK) {
-      if (std::string(ptf_batch_last_error(s->batch)).find("budget") != std::string::npos) return false;
-      q.state = REQ_FAILED; q.error = ptf_batch_last_error(s->batch); return true;
-    }
+    const int rc = ptf_batch_add(s->batch, &q.desc, q.c0.data(), u, v, &bid);
+    if (rc == PTF_ERR_MEMORY) return false;  // no room now: retry when solves retire
+    if (rc != PTF_OK) { q.state = REQ_FAILED; q.error = ptf_batch_last_error(s->batch); return true; }
     q.batch_id = bid;
   }
   q.state = REQ_ACTIVE;
@@ -143,6 +157,8 @@ void finish(ptf_server* s, int64_t id, Request& q) {
   q.state = rc ? REQ_FAILED : REQ_DONE;
   q.u.clear(); q.v.clear(); q.w.clear();
   if (!rc) {
+    q.mass_end = mass_of(q.result.data(), q.result.size());
+    if (q.mass0 != 0.0) s->mass_drift_max = std::max(s->mass_drift_max, std::fabs(q.mass_end / q.mass0 - 1.0));
     s->latencies.push_back(std::chrono::duration<double>(q.t_done - q.t_submit).count());
     s->grid_point_steps += points(q.desc) * (double)q.desc.nsteps;
     s->completed++;
@@ -151,6 +167,27 @@ void finish(ptf_server* s, int64_t id, Request& q) {
   }
   s->t_last = q.t_done;
   (void)id;
+}
+
+// A request that failed in flight: release its slot or handle so that the
+// memory budget and the batch's slots come back.
+void drop_failed(ptf_server* s, Request& q, const std::string& why) {
+  if (q.handle) {
+    int64_t hb = 0;
+    ptf_device_bytes(q.handle, &hb);
+    s->handle_bytes -= hb;
+    ptf_destroy(q.handle);
+    q.handle = nullptr;
+  } else if (q.batch_id >= 0) {
+    ptf_batch_remove(s->batch, q.batch_id);  // deactivates the slot; a sticky CUDA error leaves nothing to free
+    q.batch_id = -1;
+  }
+  q.state = REQ_FAILED;
+  q.error = why;
+  q.t_done = Clock::now();
+  q.u.clear(); q.v.clear(); q.w.clear();
+  s->failed++;
+  s->t_last = q.t_done;
 }
 
 void worker_loop(ptf_server* s) {
@@ -183,19 +220,35 @@ void worker_loop(ptf_server* s) {
       for (int64_t id : s->active)
         if (s->reqs[id].handle) handles.push_back(s->reqs[id].handle);
     }
-    // GPU work outside the lock (only this thread touches the batch and handles)
-    int rc = ptf_batch_step(s->batch, chunk);
-    for (ptf_handle* h : handles)
-      if (!rc) rc = ptf_step(h, chunk);
-    if (!rc) rc = ptf_batch_synchronize(s->batch);
+    bool injected = false;
     {
       std::lock_guard<std::mutex> lk(s->mu);
-      if (rc) s->error = ptf_batch_last_error(s->batch);
+      if (s->inject_fail_in == 0) injected = true;
+      if (s->inject_fail_in >= 0) s->inject_fail_in--;
+    }
+    // GPU work outside the lock (only this thread touches the batch and handles)
+    std::string why;
+    int rc = injected ? PTF_ERR_CUDA : ptf_batch_step(s->batch, chunk);
+    if (injected) why = "batched step: injected failure (test)";
+    else if (rc) why = std::string("batched step: ") + ptf_batch_last_error(s->batch);
+    for (ptf_handle* h : handles) {
+      if (rc) break;
+      rc = ptf_step(h, chunk);
+      if (!rc) rc = ptf_synchronize(h);
+      if (rc) why = std::string("3D step: ") + ptf_last_error(h);
+    }
+    if (!rc) {
+      rc = ptf_batch_synchronize(s->batch);
+      if (rc) why = std::string("batched step: ") + ptf_batch_last_error(s->batch);
+    }
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      if (rc) s->error = why;
       std::vector<int64_t> still;
       for (int64_t id : s->active) {
         Request& q = s->reqs[id];
+        if (rc) { drop_failed(s, q, why); continue; }
         q.done_steps = std::min<int64_t>(q.desc.nsteps, q.done_steps + chunk);
-        if (rc) { q.state = REQ_FAILED; q.error = s->error; q.t_done = Clock::now(); s->failed++; continue; }
         if (q.done_steps >= q.desc.nsteps) finish(s, id, q);
         else still.push_back(id);
       }
@@ -274,10 +327,19 @@ int ptf_server_submit(ptf_server* s, const ptf_solve_desc* d, const double* c0, 
   if (three && !(d->n >= 16 && d->n <= 256 && (d->n & (d->n - 1)) == 0))
     return sfail(s, PTF_ERR_ARG, "3D requests take n a power of two in [16, 256]");
   if (!(d->dt > 0) || d->nsteps < 1) return sfail(s, PTF_ERR_ARG, "dt must be positive and nsteps >= 1");
+  if (s->cfg.memory_budget > 0) {
+    // what this request needs in an otherwise empty server: it never fits if that exceeds the budget
+    const int64_t need = three ? (int64_t)handle_estimate(s, *d) + ptf::batch_fixed_bytes(s->batch)
+                               : ptf::batch_fixed_bytes(s->batch) + ptf::batch_slot_bytes(s->batch, d->n);
+    if (need > s->cfg.memory_budget)
+      return sfail(s, PTF_ERR_MEMORY, "request needs " + std::to_string(need) + " device bytes, more than the server's memory budget of " +
+                                          std::to_string(s->cfg.memory_budget));
+  }
   Request q;
   q.desc = *d;
   const size_t np = (size_t)points(*d);
   q.c0.assign(c0, c0 + np);
+  q.mass0 = mass_of(c0, np);
   if (d->flow_kind == PTF_FLOW_ARRAYS) {
     q.u.assign(u, u + np);
     q.v.assign(v, v + np);
@@ -356,10 +418,35 @@ int ptf_server_get_stats(ptf_server* s, ptf_server_stats* out) {
     out->mean_s = sum / (double)l.size();
   }
   out->grid_point_steps = s->grid_point_steps;
+  out->mass_drift_max_abs = s->mass_drift_max;
+  int64_t live = 0;
+  for (const auto& kv : s->reqs) if (kv.second.handle) ++live;
+  out->handles = live;
   out->wall_s = s->started && s->completed ? std::chrono::duration<double>(s->t_last - s->t_first).count() : 0.0;
-  int64_t bytes = 0;
-  ptf_batch_info(s->batch, &bytes, nullptr, nullptr);
+  int64_t bytes = 0, solves = 0;
+  ptf_batch_info(s->batch, &bytes, &solves, nullptr);
   out->device_bytes = bytes + s->handle_bytes;
+  out->batch_solves = solves;
+  return PTF_OK;
+}
+
+int ptf_server_result_info(ptf_server* s, int64_t id, double* latency_s, double* mass0, double* mass_end) {
+  if (!s) return sfail(nullptr, PTF_ERR_ARG, "null server");
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return sfail(s, PTF_ERR_ARG, "unknown request id");
+  const Request& q = it->second;
+  if (q.state != REQ_DONE) return sfail(s, PTF_ERR_STATE, "request not done");
+  if (latency_s) *latency_s = std::chrono::duration<double>(q.t_done - q.t_submit).count();
+  if (mass0) *mass0 = q.mass0;
+  if (mass_end) *mass_end = q.mass_end;
+  return PTF_OK;
+}
+
+int ptf_server_inject_step_failure(ptf_server* s, int32_t chunks_from_now) {
+  if (!s) return sfail(nullptr, PTF_ERR_ARG, "null server");
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->inject_fail_in = chunks_from_now < 0 ? -1 : chunks_from_now;
   return PTF_OK;
 }
 

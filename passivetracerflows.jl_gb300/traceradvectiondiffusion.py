@@ -418,11 +418,16 @@ class Problem:
         cfg = self._cfg
         with open(path, "wb") as f:  # exactly at ``path`` (np.savez would append ".npz")
             np.savez(f, sol=self.sol, t=t, step=step, dim=cfg.dim, nx=cfg.nx, ny=cfg.ny, nz=cfg.nz,
-                     batch=cfg.batch, dt=cfg.dt, stepper=cfg.stepper, precision=cfg.precision)
+                     batch=cfg.batch, dt=cfg.dt, stepper=cfg.stepper, precision=cfg.precision,
+                     **{k: getattr(cfg, k) for k in self._PHYSICS_KEYS})
+
+    # domain and diffusivities a checkpoint must share with the problem it resumes
+    _PHYSICS_KEYS = ("Lx", "Ly", "Lz", "kappa", "eta", "iota", "kappah", "nkappah")
 
     def load_state(self, path):
-        """Resume from ``save_state``: the grid, batch, dt, stepper and
-        precision must match this problem."""
+        """Resume from ``save_state``: the grid, batch, dt, stepper,
+        precision, domain lengths and diffusivities must match this problem
+        (a checkpoint of other physics is refused, not continued)."""
         with np.load(path) as z:
             cfg = self._cfg
             for k in ("dim", "nx", "ny", "nz", "batch", "stepper", "precision"):
@@ -430,6 +435,11 @@ class Problem:
                     raise ValueError(f"checkpoint {k}={int(z[k])} does not match this problem ({getattr(cfg, k)})")
             if float(z["dt"]) != cfg.dt:
                 raise ValueError("checkpoint dt does not match this problem")
+            for k in self._PHYSICS_KEYS:
+                if k not in z.files:
+                    raise ValueError(f"checkpoint has no {k}: written by an older version, refused")
+                if float(z[k]) != float(getattr(cfg, k)):
+                    raise ValueError(f"checkpoint {k}={float(z[k])} does not match this problem ({getattr(cfg, k)})")
             self.sol = z["sol"]
             L.check(L.load().ptf_set_clock(self._h, float(z["t"]), int(z["step"])), self._h)
         if not self.flow.steadyflow and not getattr(self, "_device_flow", False):

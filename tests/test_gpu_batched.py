@@ -146,3 +146,56 @@ def test_persistent_and_item_launches_agree(gpu, oracle, T, tol):
         b.close()
     for a, c in zip(*out):
         assert oracle.rel_l2(a, c) <= tol
+
+
+def _uniform_damping_case(gpu, oracle, n=128, nsteps=300, dt=0.002):
+    """Uniform damping (nκh = 0: L = -κh for every mode, k = 0 included) makes
+    the mean decay, so an FP32 (0,0) state's rounding would show."""
+    u, v = cellular_arrays(n)
+    x = -np.pi + 2 * np.pi / n * np.arange(n)
+    Y, X = np.meshgrid(x, x, indexing="ij")
+    c0 = 1.0 + np.exp(-((X - 1.0) ** 2 + (Y - 2.0) ** 2) / 0.18) + 0.3 * np.cos(2 * X + Y)
+    spec = gpu.SolveSpec(n=n, nsteps=nsteps, dt=dt, kappa=1e-3, kappah=0.5, nkappah=0)
+    r = oracle.Problem(oracle.TwoDAdvectingFlow(u=lambda *a: u, v=lambda *a: v), nx=n, kappa=1e-3, kappah=0.5,
+                       nkappah=0, dt=dt)
+    oracle.set_c(r, c0)
+    oracle.stepforward(r, nsteps)
+    oracle.updatevars(r)
+    return spec, c0, u, v, r
+
+
+def test_batch_k0_mode_mean_vs_oracle(gpu, oracle):
+    """FP32 batched solves carry the conserved (0,0) mode in FP64 (k0_mode, the
+    default): the mean of the result matches the FP64 oracle to 1e-9 relative
+    (the FP64 state leaves only the rounding of N(0,0) summed from FP32
+    products), the field keeps the FP32 bound 1e-5; with the mode off the mean
+    is FP32-rounded, at least ten times further off."""
+    spec, c0, u, v, r = _uniform_damping_case(gpu, oracle)
+    errs = {}
+    for k0 in (True, False):
+        b = gpu.BatchedProblem(T=np.float32, slots_per_bucket=2, k0_mode=k0)
+        ids = [b.add(spec, c0, u, v), b.add(spec, c0, u, v)]  # two slots: column 0 of each in its own lines
+        b.step(spec.nsteps)
+        cs = [b.get_c(i) for i in ids]
+        b.close()
+        for c in cs:
+            assert oracle.rel_l2(c, r.vars.c) <= 1e-5
+        errs[k0] = max(abs(c.sum() - r.vars.c.sum()) / abs(r.vars.c.sum()) for c in cs)
+    assert errs[True] <= 1e-9
+    assert errs[True] * 10 < errs[False]
+
+
+@pytest.mark.parametrize("n", [64, 256])
+def test_batch_k0_mode_sizes_and_persistent(gpu, oracle, n):
+    """Every bucket size's column layout (64: a block's lines span two slots)
+    and the persistent kernel keep the FP64 mean."""
+    spec, c0, u, v, r = _uniform_damping_case(gpu, oracle, n=n, nsteps=120)
+    for persistent in (False, True):
+        b = gpu.BatchedProblem(T=np.float32, slots_per_bucket=3, persistent=persistent)
+        ids = [b.add(spec, c0, u, v) for _ in range(3)]
+        b.step(spec.nsteps)
+        for i in ids:
+            c = b.get_c(i)
+            assert abs(c.sum() - r.vars.c.sum()) <= 1e-9 * abs(r.vars.c.sum())
+            assert oracle.rel_l2(c, r.vars.c) <= 1e-5
+        b.close()

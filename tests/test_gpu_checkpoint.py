@@ -70,3 +70,49 @@ def test_checkpoint_must_match_problem(gpu, tmp_path):
         b = _make(gpu, 2, kw["n"], kw["stepper"], kw["T"])
         with pytest.raises(ValueError):
             b.load_state(ck)
+
+
+@pytest.mark.parametrize("kw", [dict(κ=5e-3), dict(η=2e-3), dict(Lx=4.0), dict(κh=1e-8, nκh=2)])
+def test_checkpoint_of_other_physics_refused(gpu, tmp_path, kw):
+    """A checkpoint written for another domain length or diffusivity is
+    refused, not continued with physics that do not match."""
+    a = _make(gpu, 2, 64, "RK4", np.float64)
+    ck = tmp_path / "state.npz"
+    a.save_state(ck)
+    args = dict(nx=64, κ=2e-3, η=1e-3, dt=0.004, stepper="RK4", T=np.float64)
+    args.update(kw)
+    b = gpu.Problem(gpu.GPU(), _flow(gpu, 2), **args)
+    with pytest.raises(ValueError):
+        b.load_state(ck)
+
+
+def test_output_snapshots_of_a_solve(gpu, oracle, tmp_path):
+    """The reference example's output loop (Output with get_concentration,
+    saveproblem, saveoutput every 50 steps; examples/onedim_gaussiandiffusion.jl:74-88)
+    on a 1D diffusion solve: every stored snapshot equals the oracle's field at
+    that step."""
+    n, nsteps, every = 128, 200, 50
+    p = gpu.Problem(gpu.GPU(), gpu.OneDAdvectingFlow(u=lambda x: 0.0 * x), nx=n, Lx=2 * np.pi, κ=0.01, dt=0.02)
+    r = oracle.Problem(oracle.OneDAdvectingFlow(u=lambda x: 0.0 * x), nx=n, Lx=2 * np.pi, kappa=0.01, dt=0.02)
+    x = gpu.gridpoints(p.grid)
+    c0 = 0.1 * np.exp(-x ** 2 / (2 * 0.1 ** 2))
+    gpu.set_c(p, c0)
+    oracle.set_c(r, c0)
+    out = gpu.Output(p, tmp_path / "advection-diffusion1D.jld2", ("concentration", gpu.get_concentration))
+    gpu.saveproblem(out)
+    expect = {}
+    while p.clock.step <= nsteps:
+        if p.clock.step % every == 0:
+            gpu.saveoutput(out)
+            oracle.updatevars(r)
+            expect[p.clock.step] = r.vars.c.copy()
+        gpu.stepforward(p)
+        oracle.stepforward(r)
+    f = gpu.jldopen(out.path)
+    steps = sorted(int(k) for k in f["snapshots/t"].keys())
+    assert steps == [0, 50, 100, 150, 200]
+    for i in steps:
+        assert f[f"snapshots/t/{i}"] == pytest.approx(0.02 * i, abs=1e-12)
+        assert oracle.rel_l2(f[f"snapshots/concentration/{i}"], expect[i]) <= 1e-12
+    assert np.array_equal(f["grid/x"], x)
+    f.close()
