@@ -58,12 +58,16 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-oracle-check", action="store_true")
     ap.add_argument("--only-main", action="store_true", help="skip the 3D, ensemble and serving measurements")
-    ap.add_argument("--serve-requests", type=int, default=240)
+    ap.add_argument("--serve-requests", type=int, default=600)
     ap.add_argument("--serve-requests-fp64", type=int, default=48)
-    ap.add_argument("--serve-rate", type=float, default=40.0, help="Poisson arrival rate (requests/s)")
-    ap.add_argument("--ensemble-steps", type=int, default=100)
+    ap.add_argument("--serve-rate", type=float, default=12.0, help="Poisson arrival rate (requests/s)")
+    ap.add_argument("--ensemble-steps", type=int, default=1000)
+    ap.add_argument("--config-steps-2d", type=int, default=1000, help="steps of the 4096^2 configuration")
+    ap.add_argument("--config-steps-3d", type=int, default=500, help="steps of the 256^3 configuration")
+    ap.add_argument("--only", default="", help="comma-separated workload keys to run (default: all)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes (no ptf_autotune)")
-    ap.add_argument("--acc-time", type=float, default=0.1, help="simulated time of the accuracy window")
+    ap.add_argument("--acc-time", type=float, default=0.5,
+                    help="simulated time of the accuracy window (0.5 = the configured 1000 steps at dt 5e-4)")
     ap.add_argument("--no-comparator", action="store_true", help="skip the torch/cuFFT comparator")
     ap.add_argument("--profile-case", action="store_true",
                     help="only step the batched workload (for ncu); prints no result line")
@@ -113,6 +117,23 @@ def profiled_traffic(kernel, precision, n, batch):
                     and int(m.group(4)) == batch:
                 return int(m.group(5)), f.name
     return None, None
+
+
+def fft_flops_2d_rhs(nx, ny):
+    """FP64 operation count of one 2D right-hand side by the usual FFT
+    convention (5 N log2 N flops per complex transform of length N): the
+    column pass's 3 transforms per half-spectrum column (forward, two
+    inverses) and the row pass's 1.5 per row (two inverses and one forward
+    per row pair); the pointwise products (a few percent) are not counted."""
+    nkr = nx // 2 + 1
+    return 3 * nkr * 5 * ny * math.log2(ny) + 1.5 * ny * 5 * nx * math.log2(nx)
+
+
+def measure_fma_peak(lib, precision):
+    """FMA flops/s of the library's bounded probe kernel on this GPU (None if it fails)."""
+    import ctypes as ct
+    out = ct.c_double()
+    return out.value if lib.ptf_measure_fma_peak(precision, ct.byref(out)) == 0 else None
 
 
 def load_peaks():
@@ -430,12 +451,23 @@ def run_ours(args):
         prof64[name] = {"ms": ms, "launches": cnt, "bytes": by}
     lib.ptf_profile(p64._h, 0)
     clocks = sampler.stop()
+    # FP64 roof: the FP64 FMA rate of this GPU, measured by the library's probe
+    fp64_peak = measure_fma_peak(lib, 0)
+    fp64_flops_step = 4 * fft_flops_2d_rhs(n, n)
+    fp64_achieved = fp64_flops_step / (ms64 / K64 / 1e3)
+    bytes64_step = sum(x["bytes"] for x in prof64.values()) / 8  # 8 profiled steps
+    roof64 = {"bound": "fp64", "achieved": fp64_achieved / 1e12, "unit": "TFLOP/s",
+              "peak": fp64_peak / 1e12 if fp64_peak else None,
+              "peak_kind": "measured (ptf_measure_fma_peak, 2 flops per DFMA)",
+              "frac": (fp64_achieved / fp64_peak) if fp64_peak else None,
+              "flops_per_step": fp64_flops_step,
+              "flop_model": "5 N log2 N per complex FFT; 3 column + 1.5 row transforms per line per RHS; 4 RHS/step",
+              "hbm_GBps_algorithmic": bytes64_step / (ms64 / K64 / 1e3) / 1e9}
     # ---------------- accuracy vs the FP64 oracle ----------------
     # The bench's own problems, restarted from the initial condition and
-    # stepped over a fixed window (t = 0.1 at dt = 5e-4): beyond it the
-    # flow's strain has thinned the tracer below the grid scale (the
-    # workload notes), and every solution, FP64 included, is dominated by
-    # under-resolution, not by the arithmetic.
+    # stepped over the configured 1000 steps (t = 0.5 at dt = 5e-4); solve 0
+    # (the Gaussian at (pi/2, pi/2), a cell centre of the flow) is compared
+    # with the FP64 oracle.
     acc = {}
     if rank == 0 and not args.no_oracle_check:
         o = oracle_module()
@@ -511,15 +543,21 @@ def run_ours(args):
     # ---------------- other configurations (rank 0, bounded) ----------------
     workloads = {}
     if rank == 0 and not args.only_main:
-        for key, fn in (("3d_abc_256", lambda: run_abc3d_256(pkg, torch)),
+        for key, fn in (("2d_cellular_4096", lambda: run_config2_4096(pkg, torch, args.config_steps_2d)),
+                        ("3d_abc_256", lambda: run_abc3d_256(pkg, torch, args.config_steps_3d)),
                         ("ensemble_256_solves", lambda: run_ensemble_256(pkg, torch, args.ensemble_steps)),
                         ("ensemble_256_solves_clock_t",
-                         lambda: run_ensemble_256(pkg, torch, args.ensemble_steps, time_mode="clock")),
+                         lambda: run_ensemble_256(pkg, torch, args.ensemble_steps, time_mode="clock",
+                                                  fp64_check=False)),
                         ("served_fp32", lambda: run_served_stream(pkg, np.float32, args.serve_requests, args.serve_rate)),
                         ("served_fp64", lambda: run_served_stream(pkg, np.float64, args.serve_requests_fp64,
-                                                            args.serve_rate / 4))):
+                                                            args.serve_rate / 8, check=0))):
+            if args.only and key not in args.only.split(","):
+                continue
             try:
+                t_w = time.perf_counter()
                 workloads[key] = fn()
+                workloads[key]["bench_seconds"] = time.perf_counter() - t_w
             except Exception as e:  # report the failure in the line rather than losing the main result
                 workloads[key] = {"error": f"{type(e).__name__}: {e}"}
     # ---------------- CPU baseline (rank 0) ----------------
@@ -556,7 +594,8 @@ def run_ours(args):
         "config": dict(workload(args, B), parallelism="replicas" if world > 1 else "single GPU"),
         "tuning": {"fp32_batched": tuning32, "fp64_plain": tuning64},
         "fp64_plain": {"value": value64, "unit": UNIT, "ms_per_step": ms64 / K64, "steps": K64, "dtype": "f64",
-                       "passes": passes64, "ratio_fp32_batched_over_fp64": value / value64},
+                       "passes": passes64, "ratio_fp32_batched_over_fp64": value / value64, "roofline": roof64,
+                       "hbm_frac": roof64["hbm_GBps_algorithmic"] / hbm_peak},
         "accuracy": acc,
         "gpu_comparator": comparator,
         "passes": passes,
@@ -581,102 +620,209 @@ def run_ours(args):
 # ---------------------------------------------------------------------------
 # Secondary configurations (bounded samples; reported inside the one JSON line)
 # ---------------------------------------------------------------------------
-def run_abc3d_256(pkg, torch, steps=10):
+def _timed_run(pkg, torch, p, c0, steps, warm=3):
+    """set_c, `warm` untimed steps (graph capture), set_c again, then exactly
+    `steps` steps timed with CUDA events on the problem's stream; returns
+    (ms per step, vars.c after the `steps` steps)."""
+    st = torch.cuda.ExternalStream(p.stream)
+    pkg.set_c(p, c0)
+    pkg.stepforward(p, warm)
+    pkg.set_c(p, c0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    pkg.stepforward(p, steps)
+    e1.record(st)
+    e1.synchronize()
+    pkg.updatevars(p)
+    return e0.elapsed_time(e1) / steps, p.vars.c.copy()
+
+
+def _window(pkg, p, c0, steps):
+    pkg.set_c(p, c0)
+    pkg.stepforward(p, steps)
+    pkg.updatevars(p)
+    return p.vars.c.copy()
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _drift(c, m0):
+    return float(np.sum(c)) / m0 - 1.0
+
+
+def run_config2_4096(pkg, torch, steps=1000, oracle_steps=20, dt=1e-4):
+    """2D cellular flow at 4096², ETDRK4, κ=η=1e-4, κh=1e-12 (nκh=2), Gaussian
+    σ=0.2 at (π/2, π/2): one FP32 and one FP64 solve of the configured 1000
+    steps (dt = 1e-4 for an advective CFL number of 0.82; the configured 2e-3
+    gives 16 and every solution diverges), FP32 against the FP64 GPU path at
+    full length, and both against the FP64 oracle over the first
+    `oracle_steps` steps at full size."""
+    n = 4096
+    u, v = flow_fns()
+    kw = dict(nx=n, Lx=2 * np.pi, κ=1e-4, η=1e-4, κh=1e-12, nκh=2, dt=dt, stepper="ETDRK4")
+    x = -np.pi + 2 * np.pi / n * np.arange(n)
+    X, Y = np.meshgrid(x, x)
+    c0 = np.exp(-((X - np.pi / 2) ** 2 + (Y - np.pi / 2) ** 2) / (2 * 0.2 ** 2))
+    m0 = float(c0.sum())
+    out, full, win = {}, {}, {}
+    for T, name in ((np.float32, "fp32"), (np.float64, "fp64")):
+        p = pkg.Problem(pkg.GPU(), pkg.TwoDAdvectingFlow(u=u, v=v), T=T, **kw)
+        ms, full[name] = _timed_run(pkg, torch, p, c0, steps)
+        win[name] = _window(pkg, p, c0, oracle_steps)
+        out[name] = {"ms_per_step": ms, "grid_pt_steps_per_s": n * n / (ms / 1e3),
+                     "mass_drift": _drift(full[name], m0), "device_bytes": p.device_bytes}
+        del p
+        torch.cuda.empty_cache()
+    o = oracle_module()
+    r = o.Problem(o.TwoDAdvectingFlow(u=u, v=v), nx=n, Lx=2 * np.pi, kappa=1e-4, eta=1e-4, kappah=1e-12,
+                  nkappah=2, dt=dt, stepper="ETDRK4")
+    t0 = time.perf_counter()
+    o.set_c(r, c0)
+    o.stepforward(r, oracle_steps)
+    o.updatevars(r)
+    out.update({
+        "steps": steps, "dt": dt, "nominal_dt": 0.002,
+        "rel_l2_fp32_vs_fp64_gpu": _rel(full["fp32"], full["fp64"]),
+        "oracle_window": {"steps": oracle_steps, "rel_l2_fp64_vs_oracle": _rel(win["fp64"], r.vars.c),
+                          "rel_l2_fp32_vs_oracle": _rel(win["fp32"], r.vars.c),
+                          "mass_drift_fp64": _drift(win["fp64"], m0), "mass_drift_fp32": _drift(win["fp32"], m0),
+                          "mass_drift_oracle": _drift(r.vars.c, m0), "oracle_seconds": time.perf_counter() - t0},
+        "ratio_fp32_over_fp64": out["fp32"]["grid_pt_steps_per_s"] / out["fp64"]["grid_pt_steps_per_s"],
+        "workload": "2D cellular psi=cos(4x)cos(4y) 4096^2, ETDRK4, kappa=eta=1e-4, kappah=1e-12 nkappah=2, "
+                    f"dt={dt:g} (CFL 0.82)",
+    })
+    return out
+
+
+def run_abc3d_256(pkg, torch, steps=500, oracle_steps=20):
     """3D ABC flow, 256³, ETDRK4, κ=η=ι=5e-4, dt=0.005, Gaussian σ=0.3 at the
-    centre: FP32 and FP64 single solves; FP32 compared with the FP64 GPU solve."""
+    centre: FP32 and FP64 single solves of the configured 500 steps, FP32
+    against the FP64 GPU path at full length, and both against the FP64
+    oracle over the first `oracle_steps` steps at full size."""
     n, dt = 256, 0.005
     A, B, C = 1.0, np.sqrt(2 / 3), np.sqrt(1 / 3)
     u = lambda x, y, z: A * np.sin(z) + C * np.cos(y)
     v = lambda x, y, z: B * np.sin(x) + A * np.cos(z)
     w = lambda x, y, z: C * np.sin(y) + B * np.cos(x)
-    out, fields = {}, {}
+    x = -np.pi + 2 * np.pi / n * np.arange(n)
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    c0 = np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / (2 * 0.3 ** 2))
+    del X, Y, Z
+    m0 = float(c0.sum())
+    out, full, win = {}, {}, {}
     for T, name in ((np.float32, "fp32"), (np.float64, "fp64")):
         t0 = time.perf_counter()
         p = pkg.Problem(pkg.GPU(), pkg.ThreeDAdvectingFlow(u=u, v=v, w=w), nx=n, κ=5e-4, dt=dt,
                         stepper="ETDRK4", T=T)
-        X, Y, Z = pkg.gridpoints(p.grid)
-        pkg.set_c(p, np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / (2 * 0.3 ** 2)))
         setup = time.perf_counter() - t0
-        st = torch.cuda.ExternalStream(p.stream)
-        pkg.stepforward(p, 2)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        pkg.stepforward(p, steps)
-        e1.record(st)
-        e1.synchronize()
-        ms = e0.elapsed_time(e1) / steps
-        pkg.updatevars(p)
-        fields[name] = p.vars.c.copy()
+        ms, full[name] = _timed_run(pkg, torch, p, c0, steps)
+        win[name] = _window(pkg, p, c0, oracle_steps)
         out[name] = {"ms_per_step": ms, "grid_pt_steps_per_s": n ** 3 / (ms / 1e3), "setup_s": setup,
-                     "device_bytes": p.device_bytes}
+                     "mass_drift": _drift(full[name], m0), "device_bytes": p.device_bytes}
         del p
         torch.cuda.empty_cache()
-    d = fields["fp32"] - fields["fp64"]
-    out["rel_l2_fp32_vs_fp64_gpu"] = float(np.linalg.norm(d) / np.linalg.norm(fields["fp64"]))
-    out["steps"] = 2 + steps
-    out["workload"] = "3D ABC flow 256^3, ETDRK4, kappa=5e-4, dt=0.005"
+    o = oracle_module()
+    r = o.Problem(o.ThreeDAdvectingFlow(u=u, v=v, w=w), nx=n, kappa=5e-4, dt=dt, stepper="ETDRK4")
+    t0 = time.perf_counter()
+    o.set_c(r, c0)
+    o.stepforward(r, oracle_steps)
+    o.updatevars(r)
+    out.update({
+        "steps": steps, "rel_l2_fp32_vs_fp64_gpu": _rel(full["fp32"], full["fp64"]),
+        "oracle_window": {"steps": oracle_steps, "rel_l2_fp64_vs_oracle": _rel(win["fp64"], r.vars.c),
+                          "rel_l2_fp32_vs_oracle": _rel(win["fp32"], r.vars.c),
+                          "mass_drift_fp64": _drift(win["fp64"], m0), "mass_drift_fp32": _drift(win["fp32"], m0),
+                          "mass_drift_oracle": _drift(r.vars.c, m0), "oracle_seconds": time.perf_counter() - t0},
+        "workload": "3D ABC flow 256^3, ETDRK4, kappa=eta=iota=5e-4, dt=0.005, Gaussian sigma=0.3 at the centre",
+    })
     return out
 
 
-def run_ensemble_256(pkg, torch, steps, seed=2024, time_mode="stage"):
+def run_ensemble_256(pkg, torch, steps, seed=2024, time_mode="stage", fp64_check=True, oracle_solves=4):
     """Batched ensemble: 256 2D solves, n uniform in {64,128,256,512}, κ
     log-uniform in [1e-4,1e-2], ψ = cos(x + 0.3 sin t) cos y re-evaluated at
     every RK4 stage (time_mode "stage") or frozen at clock.t for the step as
     the reference does ("clock"), Gaussian blobs (random centres, σ ∈
-    [0.1,0.5]), RK4, dt=0.005, FP32; one persistent kernel per stage, steps
-    from a CUDA graph."""
+    [0.1,0.5]), RK4, dt=0.005, FP32 with each solve's (0,0) mode in FP64; a
+    row and a column launch per stage, steps from a CUDA graph.  Every
+    solve's result is compared with the same ensemble run by the FP64
+    batched engine (the oracle for all 256 solves of 1000 steps would take
+    hours of CPU), and the `oracle_solves` smallest-κ 64² solves with the
+    FP64 oracle; mass drift of every solve against its FP64 twin."""
     rng = np.random.default_rng(seed)
-    b = pkg.BatchedProblem(T=np.float32, slots_per_bucket=96)
     sizes = rng.choice([64, 128, 256, 512], size=256)
-    specs = []
-    t0 = time.perf_counter()
-    for i, n in enumerate(sizes):
+    cases = []
+    for n in sizes:
         n = int(n)
         κ = float(10 ** rng.uniform(-4, -2))
         x0, y0 = rng.uniform(-np.pi, np.pi, 2)
         sig = float(rng.uniform(0.1, 0.5))
-        c0 = initial_gaussian(n, x0, y0, sig)
-        spec = pkg.SolveSpec(n=n, nsteps=10 ** 6, dt=0.005, kappa=κ, flow="cellular", time_mode=time_mode,
+        cases.append((n, κ, initial_gaussian(n, x0, y0, sig)))
+
+    def spec(n, κ):
+        return pkg.SolveSpec(n=n, nsteps=steps, dt=0.005, kappa=κ, flow="cellular", time_mode=time_mode,
                              U=1.0, eps=0.3, omega=1.0, Kx=1, Ky=1)
-        specs.append((b.add(spec, c0), n, κ, c0))
-    setup = time.perf_counter() - t0
-    st = torch.cuda.ExternalStream(b.stream)
-    b.step(3)  # warm-up (captures the graph)
-    b.synchronize()
-    l0 = b.info()["kernel_launches"]
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(st)
-    b.step(steps)
-    e1.record(st)
-    e1.synchronize()
-    b.synchronize()
-    ms = e0.elapsed_time(e1)
-    pts = float(sum(n * n for _, n, _, _ in specs))
-    res = {"solves": len(specs), "sizes": {str(k): int((sizes == k).sum()) for k in (64, 128, 256, 512)},
+
+    def run(T):
+        b = pkg.BatchedProblem(T=T, slots_per_bucket=96)
+        t0 = time.perf_counter()
+        ids = [b.add(spec(n, κ), c0) for n, κ, c0 in cases]
+        setup = time.perf_counter() - t0
+        st = torch.cuda.ExternalStream(b.stream)
+        b.synchronize()
+        l0 = b.info()["kernel_launches"]
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        b.step(steps)  # the first step captures the graph: inside the timed region
+        e1.record(st)
+        e1.synchronize()
+        b.synchronize()
+        ms = e0.elapsed_time(e1)
+        info = b.info()
+        fields = [b.get_c(i) for i in ids]
+        b.close()
+        torch.cuda.empty_cache()
+        return ms, setup, (info["kernel_launches"] - l0) / steps, info["device_bytes"], fields
+
+    ms, setup, lps, dev_bytes, f32 = run(np.float32)
+    pts = float(sum(n * n for n, _, _ in cases))
+    m0 = [float(c0.sum()) for _, _, c0 in cases]
+    res = {"solves": len(cases), "sizes": {str(k): int((sizes == k).sum()) for k in (64, 128, 256, 512)},
            "steps": steps, "ms_per_step": ms / steps, "grid_pt_steps_per_s": pts * steps / (ms / 1e3),
-           "setup_s": setup, "graph_replays": steps, "launches_per_step": (b.info()["kernel_launches"] - l0) / steps,
-           "device_bytes": b.info()["device_bytes"],
-           "workload": f"256 solves n in {{64..512}}, RK4 dt=0.005, cellular psi=cos(x+0.3 sin t)cos y at "
-                       f"{'stage times' if time_mode == 'stage' else 'clock.t (frozen per step)'}, FP32"}
-    # accuracy: the two smallest-κ 64² solves against the oracle (stage-time flow)
-    try:
+           "setup_s": setup, "launches_per_step": lps, "device_bytes": dev_bytes,
+           "mass_drift_fp32_max_abs": max(abs(_drift(c, m)) for c, m in zip(f32, m0)),
+           "workload": f"256 solves n in {{64..512}}, RK4 dt=0.005, {steps} steps, cellular psi=cos(x+0.3 sin t)cos y at "
+                       f"{'stage times' if time_mode == 'stage' else 'clock.t (frozen per step)'}, FP32 with FP64 k=0 mode"}
+    if fp64_check:
+        ms64, _, _, _, f64 = run(np.float64)
+        rel = [_rel(a, b) for a, b in zip(f32, f64)]
+        dd = [abs(_drift(a, m) - _drift(b, m)) for a, b, m in zip(f32, f64, m0)]
+        res["fp64_batched"] = {"ms_per_step": ms64 / steps, "grid_pt_steps_per_s": pts * steps / (ms64 / 1e3)}
+        res["rel_l2_fp32_vs_fp64_gpu"] = {"max": max(rel), "median": float(np.median(rel)),
+                                          "solves_over_1e-5": int(sum(r > 1e-5 for r in rel))}
+        res["mass_drift_fp32_minus_fp64_max_abs"] = max(dd)
+        res["mass_drift_fp64_max_abs"] = max(abs(_drift(c, m)) for c, m in zip(f64, m0))
+    if oracle_solves:
         o = oracle_module()
-        picks = sorted([s for s in specs if s[1] == 64], key=lambda s: s[2])[:2]
-        errs = []
-        for sid, n, κ, c0 in picks:
-            uu = lambda x, y, t: np.cos(x + 0.3 * np.sin(t)) * np.sin(y)
-            vv = lambda x, y, t: -np.sin(x + 0.3 * np.sin(t)) * np.cos(y)
+        picks = sorted([i for i, (n, _, _) in enumerate(cases) if n == 64], key=lambda i: cases[i][1])[:oracle_solves]
+        uu = lambda x, y, t: np.cos(x + 0.3 * np.sin(t)) * np.sin(y)
+        vv = lambda x, y, t: -np.sin(x + 0.3 * np.sin(t)) * np.cos(y)
+        errs, drifts = [], []
+        t0 = time.perf_counter()
+        for i in picks:
+            n, κ, c0 = cases[i]
             r = o.Problem(o.TwoDAdvectingFlow(u=uu, v=vv, steadyflow=False), nx=n, kappa=κ, dt=0.005,
                           stage_time=(time_mode == "stage"))
             o.set_c(r, c0)
-            o.stepforward(r, 3 + steps)
+            o.stepforward(r, steps)
             o.updatevars(r)
-            errs.append(o.rel_l2(b.get_c(sid), r.vars.c))
-        res["rel_l2_fp32_vs_oracle_64x64"] = errs
-    except Exception as e:  # the oracle needs scipy; report instead of failing the bench
-        res["oracle_check"] = f"skipped: {e}"
-    b.close()
-    torch.cuda.empty_cache()
+            errs.append(_rel(f32[i], r.vars.c))
+            drifts.append(abs(_drift(f32[i], m0[i]) - _drift(r.vars.c, m0[i])))
+        res["oracle_check"] = {"solves": [f"64^2 kappa={cases[i][1]:.2e}" for i in picks], "steps": steps,
+                               "rel_l2_fp32_vs_oracle": errs, "mass_drift_vs_oracle_max_abs": max(drifts),
+                               "oracle_seconds": time.perf_counter() - t0}
     return res
 
 
@@ -717,61 +863,106 @@ def random_phase_flow(n, rng, dim=2, kmin=4, kmax=16, L=2 * np.pi):
     return u / rms, v / rms, w / rms
 
 
-def run_served_stream(pkg, T, nreq, rate, seed=5150):
-    """Served stream: requests with Poisson arrivals; each a 2D grid from
-    {64²..1024²} or 3D 128³ (one in ten), steps log-uniform in [100,5000], κ
-    log-uniform in [1e-4,1e-2], random-phase flow; dt per request for an
-    advective CFL of 0.5 and a diffusive number of 1 (RK4)."""
+def run_served_stream(pkg, T, nreq, rate, seed=5150, pool=8, check=8, max_queued=256):
+    """Served stream: requests with Poisson arrivals at `rate` per second; each
+    a 2D grid from {64²..1024²} or 3D 128³ (one in ten), steps log-uniform in
+    [100,5000], κ log-uniform in [1e-4,1e-2], random-phase incompressible
+    flow (|k| in [4,16], |û| ∝ |k|^-3, rms 1); dt per request for an advective
+    CFL of 0.5 and a diffusive number of 1 (RK4).  Flows come from a seeded
+    pool of `pool` per grid size (input generation is not what is measured).
+    The feeder holds back while `max_queued` requests wait (bounded host
+    memory; counted in `feeder_holds`).  Every result's mass drift comes from
+    the server's per-request record; `check` seeded requests (n <= 256) are
+    re-run alone through an FP64 single-solve handle and compared."""
     import threading
     rng = np.random.default_rng(seed)
-    reqs = []
     t_prep = time.perf_counter()
+    flows = {}
+    for n in (64, 128, 256, 512, 1024):
+        flows[(2, n)] = [random_phase_flow(n, rng, dim=2) for _ in range(pool)]
+    flows[(3, 128)] = [random_phase_flow(128, rng, dim=3) for _ in range(max(2, pool // 2))]
+    reqs = []
     for i in range(nreq):
         three = rng.random() < 0.1
         n = 128 if three else int(rng.choice([64, 128, 256, 512, 1024]))
         nsteps = int(10 ** rng.uniform(2, np.log10(5000)))
         κ = float(10 ** rng.uniform(-4, -2))
-        flow = random_phase_flow(n, rng, dim=3 if three else 2)
-        umax = max(float(np.abs(f).max()) for f in flow)
+        fl = flows[(3 if three else 2, n)]
+        k = int(rng.integers(len(fl)))
+        umax = max(float(np.abs(f).max()) for f in fl[k])
         kmax = n / 2
         dt = min(0.5 / (umax * kmax), 1.0 / (κ * (3 if three else 2) * kmax ** 2))
         x0 = rng.uniform(-np.pi, np.pi, 3)
         sig = float(rng.uniform(0.1, 0.5))
-        if three:
-            x = -np.pi + 2 * np.pi / n * np.arange(n)
-            Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
-            c0 = np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / (2 * sig ** 2))
-        else:
-            c0 = initial_gaussian(n, x0[0], x0[1], sig)
-        spec = pkg.SolveSpec(n=n, dim=3 if three else 2, nsteps=nsteps, dt=dt, kappa=κ)
-        reqs.append((spec, c0, flow))
+        reqs.append((three, n, nsteps, κ, dt, k, x0, sig))
     prep = time.perf_counter() - t_prep
+    x128 = -np.pi + 2 * np.pi / 128 * np.arange(128)
+    Z, Y, X = np.meshgrid(x128, x128, x128, indexing="ij")
+    r3 = X ** 2 + Y ** 2 + Z ** 2
+    del X, Y, Z
+
+    def inputs(req):
+        three, n, nsteps, κ, dt, k, x0, sig = req
+        spec = pkg.SolveSpec(n=n, dim=3 if three else 2, nsteps=nsteps, dt=dt, kappa=κ)
+        c0 = np.exp(-r3 / (2 * sig ** 2)) if three else initial_gaussian(n, x0[0], x0[1], sig)
+        return spec, c0, flows[(3 if three else 2, n)][k]
+
     srv = pkg.Server(T=T, chunk_steps=50, slots_per_bucket=32)
     gaps = rng.exponential(1.0 / rate, size=nreq)
-    ids = []
+    ids = [None] * nreq
+    holds = [0]
 
     def feeder():
         t_next = time.perf_counter()
-        for (spec, c0, flow), g in zip(reqs, gaps):
+        for i, (req, g) in enumerate(zip(reqs, gaps)):
             t_next += g
             dt_wait = t_next - time.perf_counter()
             if dt_wait > 0:
                 time.sleep(dt_wait)
-            ids.append(srv.submit(spec, c0, *flow))
+            while srv.stats()["queued"] >= max_queued:
+                holds[0] += 1
+                time.sleep(0.01)
+            spec, c0, flow = inputs(req)
+            ids[i] = srv.submit(spec, c0, *flow)
 
     t0 = time.perf_counter()
     th = threading.Thread(target=feeder)
     th.start()
     th.join()
-    srv.wait_all(1800)
+    srv.wait_all(7200)
     wall = time.perf_counter() - t0
     st = srv.stats()
+    drifts = [srv.result_info(i)["mass_drift"] for i in ids]
+    chk = {}
+    if check:
+        picks = [i for i in range(nreq) if reqs[i][1] <= 256 and not reqs[i][0]][:check]
+        errs, dd = [], []
+        for i in picks:
+            spec, c0, (u, v) = inputs(reqs[i])
+            _, c = srv.poll(ids[i])
+            p = pkg.Problem(pkg.GPU(), pkg.TwoDAdvectingFlow(), nx=spec.n, κ=spec.kappa, η=spec.kappa, dt=spec.dt,
+                            T=np.float64)
+            p.set_flow_arrays(u, v)
+            pkg.set_c(p, c0)
+            pkg.stepforward(p, spec.nsteps)
+            pkg.updatevars(p)
+            errs.append(_rel(c, p.vars.c))
+            m0 = float(c0.sum())
+            dd.append(abs(_drift(c, m0) - _drift(p.vars.c, m0)))
+            del p
+        chk = {"requests": len(picks), "what": "result vs the same request run alone by an FP64 single-solve handle",
+               "rel_l2_max": max(errs) if errs else None, "rel_l2_median": float(np.median(errs)) if errs else None,
+               "mass_drift_diff_max_abs": max(dd) if dd else None}
     srv.close()
+    work = sum(r[1] ** (3 if r[0] else 2) * r[2] for r in reqs)
     return {"requests": nreq, "arrival_rate_per_s": rate, "completed": st["completed"], "failed": st["failed"],
             "p50_latency_s": st["p50_s"], "p99_latency_s": st["p99_s"], "mean_latency_s": st["mean_s"],
-            "grid_pt_steps_per_s": st["grid_point_steps"] / wall, "wall_s": wall,
-            "peak_device_bytes": st["device_bytes"], "input_prep_s": prep,
-            "mix": "2D n in {64..1024} (90%), 3D 128^3 (10%); steps log-uniform [100,5000]; kappa log-uniform [1e-4,1e-2]"}
+            "grid_pt_steps_per_s": st["grid_point_steps"] / wall, "wall_s": wall, "total_grid_pt_steps": work,
+            "peak_device_bytes": st["device_bytes"], "input_prep_s": prep, "feeder_holds": holds[0],
+            "mass_drift_max_abs": max(abs(d) for d in drifts), "mass_drift_median_abs": float(np.median(np.abs(drifts))),
+            "fp64_check": chk,
+            "mix": "2D n in {64..1024} (90%), 3D 128^3 (10%); steps log-uniform [100,5000]; kappa log-uniform "
+                   "[1e-4,1e-2]; RK4; flows from a seeded pool of %d per size" % pool}
 
 
 def ct_read(lib, h, kind):

@@ -196,6 +196,11 @@ int ptf_profile_read(ptf_handle* h, int32_t kind, double* total_ms, int64_t* lau
 /* Kernels launched by this handle since creation (for launch accounting). */
 int ptf_kernel_launches(const ptf_handle* h, int64_t* count);
 int32_t ptf_abi_version(void);
+/* Arithmetic throughput of the current device (no reference counterpart):
+ * FMA flops per second (2 per FMA) of a bounded probe kernel in precision
+ * PTF_FP64 or PTF_FP32 -- the roof that bounds the FP64 path, whose FFT
+ * butterflies issue on this chip's narrow FP64 pipe, not on HBM. */
+int ptf_measure_fma_peak(int32_t precision, double* flops_per_s);
 
 /* ---------------------------------------------------------------------------
  * Batched form.  No single reference counterpart: the reference runs one

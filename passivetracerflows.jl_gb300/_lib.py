@@ -92,6 +92,7 @@ class PtfArgumentError(PtfError, ValueError):
 # name -> (restype, argtypes)
 SIGNATURES = {
     "ptf_abi_version": (ct.c_int32, []),
+    "ptf_measure_fma_peak": (ct.c_int, [ct.c_int32, ct.POINTER(ct.c_double)]),
     "ptf_config_default": (None, [ct.POINTER(PtfConfig), ct.c_int32]),
     "ptf_create": (ct.c_int, [ct.POINTER(PtfConfig), ct.POINTER(ct.c_void_p)]),
     "ptf_destroy": (None, [ct.c_void_p]),

@@ -231,10 +231,16 @@ void worker_loop(ptf_server* s) {
     int rc = injected ? PTF_ERR_CUDA : ptf_batch_step(s->batch, chunk);
     if (injected) why = "batched step: injected failure (test)";
     else if (rc) why = std::string("batched step: ") + ptf_batch_last_error(s->batch);
+    // 3D handles: enqueue every handle's chunk (their streams run beside the
+    // batch's), then wait for each
     for (ptf_handle* h : handles) {
       if (rc) break;
       rc = ptf_step(h, chunk);
-      if (!rc) rc = ptf_synchronize(h);
+      if (rc) why = std::string("3D step: ") + ptf_last_error(h);
+    }
+    for (ptf_handle* h : handles) {
+      if (rc) break;
+      rc = ptf_synchronize(h);
       if (rc) why = std::string("3D step: ") + ptf_last_error(h);
     }
     if (!rc) {
