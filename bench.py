@@ -962,7 +962,7 @@ def run_served_stream(pkg, T, nreq, rate, seed=5150, pool=8, check=8, max_queued
             "mass_drift_max_abs": max(abs(d) for d in drifts), "mass_drift_median_abs": float(np.median(np.abs(drifts))),
             "fp64_check": chk,
             "mix": "2D n in {64..1024} (90%), 3D 128^3 (10%); steps log-uniform [100,5000]; kappa log-uniform "
-                   "[1e-4,1e-2]; RK4; flows from a seeded pool of %d per size" % pool}
+                   f"[1e-4,1e-2]; RK4; flows from a seeded pool of {pool} per size"}
 
 
 def ct_read(lib, h, kind):

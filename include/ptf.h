@@ -271,6 +271,15 @@ int ptf_batch_get_c(ptf_batch* b, int64_t id, double* c);
 int ptf_batch_remove(ptf_batch* b, int64_t id);
 int ptf_batch_info(ptf_batch* b, int64_t* device_bytes, int64_t* solves, int64_t* kernel_launches);
 int ptf_batch_get_stream(const ptf_batch* b, void** stream);
+/* Failure-detection test hook (no reference counterpart), persistent form
+ * only: from the next step, a column item of the persistent stage kernel
+ * waits for extra_row_items more row items of its bucket than exist, so its
+ * bounded wait runs out after spin_limit sleeps of about 128 ns (0: the
+ * default limit, about 2 s); the item is skipped, the kernel ends, and
+ * ptf_batch_synchronize returns PTF_ERR_CUDA.  Nothing traps or faults and
+ * the CUDA context stays usable; the batch's results are invalid from then
+ * on.  extra_row_items = 0 restores the normal wait. */
+int ptf_batch_inject_wait_timeout(ptf_batch* b, int32_t extra_row_items, int64_t spin_limit);
 
 /* ---------------------------------------------------------------------------
  * Request server (no reference counterpart): continuous batching.  A worker

@@ -122,6 +122,7 @@ SIGNATURES = {
     "ptf_batch_add": (ct.c_int, [ct.c_void_p, ct.POINTER(PtfSolveDesc), ct.c_void_p, ct.c_void_p, ct.c_void_p,
                                  ct.POINTER(ct.c_int64)]),
     "ptf_batch_step": (ct.c_int, [ct.c_void_p, ct.c_int64]),
+    "ptf_batch_inject_wait_timeout": (ct.c_int, [ct.c_void_p, ct.c_int32, ct.c_int64]),
     "ptf_batch_synchronize": (ct.c_int, [ct.c_void_p]),
     "ptf_batch_status": (ct.c_int, [ct.c_void_p, ct.c_int64, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_double),
                                     ct.POINTER(ct.c_int32)]),

@@ -120,6 +120,12 @@ class BatchedProblem:
     def synchronize(self):
         self._check(L.load().ptf_batch_synchronize(self._h))
 
+    def inject_wait_timeout(self, extra_row_items=1, spin_limit=0):
+        """Failure-detection test hook (persistent form): column items wait for
+        row items that do not exist until their bounded wait runs out; the next
+        ``synchronize`` raises.  Nothing faults on the GPU."""
+        self._check(L.load().ptf_batch_inject_wait_timeout(self._h, int(extra_row_items), int(spin_limit)))
+
     def status(self, sid):
         st, t, act = ct.c_int64(), ct.c_double(), ct.c_int32()
         self._check(L.load().ptf_batch_status(self._h, sid, ct.byref(st), ct.byref(t), ct.byref(act)))

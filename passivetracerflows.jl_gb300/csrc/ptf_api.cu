@@ -278,7 +278,9 @@ template <typename T> int upload_tables(ptf_handle* h) {
       const double Lv = L[((size_t)q * ny + j) * pitch + k];
       double ph[4];
       etd_phis(dt * Lv, ph);
-      const double vals[6] = {std::exp(dt * Lv), std::exp(dt * Lv / 2), dt * ph[0], dt * ph[1], dt * ph[2], dt * ph[3]};
+      // E - 1 and E2 - 1 (expm1): the stage combination applies s + (E - 1) s
+      const double vals[6] = {std::expm1(dt * Lv), std::expm1(dt * Lv / 2), dt * ph[0], dt * ph[1], dt * ph[2],
+                              dt * ph[3]};
       const int js[2] = {j, (ny - j) % ny};
       const int qs[2] = {q, (nz - q) % nz};
       for (int a = 0; a < 2; ++a)

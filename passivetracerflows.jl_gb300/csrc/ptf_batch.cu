@@ -117,6 +117,8 @@ struct ptf_batch {
   long long next_id = 1;
   bool plan_dirty = true;
   long long bucket_gen = 0, plan_gen = -1;  // bumped when a bucket's buffers change
+  unsigned long long spin_limit = 0;         // persistent kernel's bounded wait (0: default)
+  unsigned int wait_extra = 0;               // test hook: row items a column item waits for beyond the real ones
   int plan_total = 0, plan_row_total = 0;
   std::vector<int> plan_lists;      // active slots per bucket of the current plan
   std::vector<int> plan_buckets;
@@ -459,6 +461,8 @@ template <typename T> int build_plan(ptf_batch* b) {
   b->plan_buckets = pbk;
   b->plan_gen = b->bucket_gen;
   plan.nb = nb;
+  plan.spin_limit = b->spin_limit;
+  plan.wait_extra = b->wait_extra;
   int off = 0;
   for (int i = 0; i < nb; ++i) { plan.b[i].row_begin = off; off += plan.b[i].row_items; }
   plan.row_total = off;
@@ -834,6 +838,17 @@ int ptf_batch_info(ptf_batch* b, int64_t* device_bytes, int64_t* solves, int64_t
   if (device_bytes) *device_bytes = (int64_t)b->bytes;
   if (solves) *solves = (int64_t)b->solves.size();
   if (launches) *launches = b->launches;
+  return PTF_OK;
+}
+
+int ptf_batch_inject_wait_timeout(ptf_batch* b, int32_t extra_row_items, int64_t spin_limit) {
+  if (!b) return bfail(nullptr, PTF_ERR_ARG, "null batch");
+  if (extra_row_items < 0 || spin_limit < 0) return bfail(b, PTF_ERR_ARG, "extra_row_items and spin_limit must be >= 0");
+  if (!b->cfg.persistent) return bfail(b, PTF_ERR_STATE, "the bounded wait exists in the persistent form only");
+  b->wait_extra = (unsigned)extra_row_items;
+  b->spin_limit = (unsigned long long)spin_limit;
+  b->plan_dirty = true;
+  b->bucket_gen++;  // rebuild the plan and the captured step with the new wait
   return PTF_OK;
 }
 

@@ -20,6 +20,11 @@ template <typename T> struct BucketPlan {
 };
 template <typename T> struct BatchPlan {
   int nb, row_total, total;
+  // bounded wait of the persistent kernel: sleeps of about 128 ns before a
+  // column item gives up (0: kSpinLimit), and extra row items a column item
+  // waits for (0; > 0 only through the test hook that makes the wait run out)
+  unsigned long long spin_limit;
+  unsigned int wait_extra;
   BucketPlan<T> b[kMaxBuckets];
 };
 
@@ -87,11 +92,12 @@ batch_stage_kernel(const BatchPlan<T>* __restrict__ plan, unsigned int* ctr, int
       int b = 0;
       while (b + 1 < nb && item >= plan->b[b + 1].col_begin) ++b;
       if (threadIdx.x == 0) {
-        const unsigned need = (unsigned)plan->b[b].row_items;
+        const unsigned need = (unsigned)plan->b[b].row_items + plan->wait_extra;
+        const unsigned long long limit = plan->spin_limit ? plan->spin_limit : kSpinLimit;
         unsigned long long spins = 0;
         int ok = 1;
         while (*((volatile unsigned int*)&ctr[1 + b]) < need) {
-          if (++spins > kSpinLimit) { atomicExch(err, 1); ok = 0; break; }
+          if (++spins > limit) { atomicExch(err, 1); ok = 0; break; }
           __nanosleep(128);
         }
         __threadfence();

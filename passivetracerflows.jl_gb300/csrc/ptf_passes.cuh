@@ -229,8 +229,12 @@ __device__ __forceinline__ double column0_sum_lines(const C* v, int w, int t, bo
 }
 
 // Stepper stage combination at one spectral element o (FourierFlows RK4;
-// Cox-Matthews ETDRK4 with coefficient planes E, E2, zeta, alpha, beta,
-// gamma at cf[o + e*plane]).  Nh = the RHS transform N(stage input) here;
+// Cox-Matthews ETDRK4 with coefficient planes E - 1, E2 - 1, zeta, alpha,
+// beta, gamma at cf[o + e*plane]: E = exp(L dt) and E2 = exp(L dt / 2) are
+// held as expm1 values and applied as s + (E - 1) s, which keeps the
+// relative accuracy of the small decay 1 - E of the slowly damped modes in
+// an FP32 table -- rounding E itself near 1 to FP32 misstates that decay by
+// up to several percent, an error that grows linearly with the steps).  Nh = the RHS transform N(stage input) here;
 // returns the next stage input (or the new state after stage 4) and updates
 // the state arrays S (sol), SI (RK4 stage input / ETDRK4 d = E2 a - zeta N(sol)),
 // AC (accumulator).  RK4 stores only when `store` (batched slots); Lf() gives
@@ -281,20 +285,20 @@ __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S,
     // a = E2 s + zeta N(s) is the next input; stage 3's
     // c = E2 a + zeta (2 N(b) - N(s)) = d + 2 zeta N(b) needs only
     // d = E2 a - zeta N(s), stored in SI in place of a and N(s)
-    const T Ee = cf[o], E2 = cf[o + plane], ze = cf[o + 2 * plane], al = cf[o + 3 * plane];
+    const T Em = cf[o], E2m = cf[o + plane], ze = cf[o + 2 * plane], al = cf[o + 3 * plane];
     const C s = ldS();
-    C ac; ac.x = Ee * s.x + al * Nh.x; ac.y = Ee * s.y + al * Nh.y;
+    C ac; ac.x = (s.x + Em * s.x) + al * Nh.x; ac.y = (s.y + Em * s.y) + al * Nh.y;
     AC[o] = ac;
-    x.x = E2 * s.x + ze * Nh.x; x.y = E2 * s.y + ze * Nh.y;
-    C d; d.x = E2 * x.x - ze * Nh.x; d.y = E2 * x.y - ze * Nh.y;
+    x.x = (s.x + E2m * s.x) + ze * Nh.x; x.y = (s.y + E2m * s.y) + ze * Nh.y;
+    C d; d.x = (x.x + E2m * x.x) - ze * Nh.x; d.y = (x.y + E2m * x.y) - ze * Nh.y;
     SI[o] = d;
   } else if (MODE == COL_ETD_2) {
-    const T E2 = cf[o + plane], ze = cf[o + 2 * plane], be = cf[o + 4 * plane];
+    const T E2m = cf[o + plane], ze = cf[o + 2 * plane], be = cf[o + 4 * plane];
     const C s = ldS();
     C ac = ldAC();
     ac.x += 2 * be * Nh.x; ac.y += 2 * be * Nh.y;
     AC[o] = ac;
-    x.x = E2 * s.x + ze * Nh.x; x.y = E2 * s.y + ze * Nh.y;
+    x.x = (s.x + E2m * s.x) + ze * Nh.x; x.y = (s.y + E2m * s.y) + ze * Nh.y;
   } else if (MODE == COL_ETD_3) {
     const T ze = cf[o + 2 * plane], be = cf[o + 4 * plane];
     const C d = ldSI();
@@ -396,7 +400,12 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
   // the combination's first state operand, fetched into this thread's park
   // slots while the forward transform runs (the slots are free until the
   // combination writes the next stage input there)
-  constexpr int PF = (PTF_EARLY_OPERAND && !BATCHED) ? early_operand(MODE) : 0;
+  // (batched form too: a thread of an inactive slot fetches from a valid
+  // slot, in bounds, and writes nothing)
+#ifndef PTF_EARLY_OPERAND_BATCHED
+#define PTF_EARLY_OPERAND_BATCHED 1
+#endif
+  constexpr int PF = (PTF_EARLY_OPERAND && (!BATCHED || PTF_EARLY_OPERAND_BATCHED)) ? early_operand(MODE) : 0;
   if (PF) {
     const C* __restrict__ op = (PF == 1 ? a.s : PF == 2 ? a.si : a.acc) + boff;
 #pragma unroll

