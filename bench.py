@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--config-steps-2d", type=int, default=1000, help="steps of the 4096^2 configuration")
     ap.add_argument("--config-steps-3d", type=int, default=500, help="steps of the 256^3 configuration")
     ap.add_argument("--only", default="", help="comma-separated workload keys to run (default: all)")
+    ap.add_argument("--workloads-only", action="store_true",
+                    help="run only the secondary configurations (no contract line)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes (no ptf_autotune)")
     ap.add_argument("--acc-time", type=float, default=0.5,
                     help="simulated time of the accuracy window (0.5 = the configured 1000 steps at dt 5e-4)")
@@ -541,8 +543,17 @@ def run_ours(args):
     e2e_val = job_rate(world, B * n * n * frames * S, e2e_s)
     bytes_field = B * n * n * 8
     # ---------------- other configurations (rank 0, bounded) ----------------
+    workloads = run_workloads(args, pkg, torch) if rank == 0 and not args.only_main else {}
+    # ---------------- CPU baseline (rank 0) ----------------
+    return _finish_ours(args, world, rank, value, ms32, K, W, B, n, dt, launches, prof, prof64, tuning32, tuning64,
+                        value64, ms64, K64, roof64, acc, comparator, e2e_val, frames, S, bytes_field, clocks, workloads)
+
+
+def run_workloads(args, pkg, torch):
+    """The secondary configurations (rank 0): each entry carries its own
+    timing, accuracy and the seconds it took; a failure is reported in place."""
     workloads = {}
-    if rank == 0 and not args.only_main:
+    if True:
         for key, fn in (("2d_cellular_4096", lambda: run_config2_4096(pkg, torch, args.config_steps_2d)),
                         ("3d_abc_256", lambda: run_abc3d_256(pkg, torch, args.config_steps_3d)),
                         ("ensemble_256_solves", lambda: run_ensemble_256(pkg, torch, args.ensemble_steps)),
@@ -560,7 +571,12 @@ def run_ours(args):
                 workloads[key]["bench_seconds"] = time.perf_counter() - t_w
             except Exception as e:  # report the failure in the line rather than losing the main result
                 workloads[key] = {"error": f"{type(e).__name__}: {e}"}
-    # ---------------- CPU baseline (rank 0) ----------------
+    return workloads
+
+
+def _finish_ours(args, world, rank, value, ms32, K, W, B, n, dt, launches, prof, prof64, tuning32, tuning64,
+                 value64, ms64, K64, roof64, acc, comparator, e2e_val, frames, S, bytes_field, clocks, workloads):
+    import torch
     cpu = None
     if rank == 0 and not args.no_cpu:
         rate, steps, el, cores = cpu_oracle_rate(args, args.cpu_seconds, 200)
@@ -650,6 +666,16 @@ def _rel(a, b):
 
 def _drift(c, m0):
     return float(np.sum(c)) / m0 - 1.0
+
+
+def _bounded(c, c0):
+    """A result that stayed a tracer field: finite, and no larger than twice
+    the initial maximum (advection-diffusion keeps max|c| <= max|c0|; small
+    spectral over- and undershoots aside)."""
+    return bool(np.all(np.isfinite(c))) and float(np.abs(c).max()) <= 2.0 * float(np.abs(c0).max())
+
+
+RK4_REAL_AXIS_LIMIT = 2.785  # RK4's stability interval on the negative real axis: dt*|L| <= 2.785
 
 
 def run_config2_4096(pkg, torch, steps=1000, oracle_steps=20, dt=1e-4):
@@ -789,21 +815,34 @@ def run_ensemble_256(pkg, torch, steps, seed=2024, time_mode="stage", fp64_check
     ms, setup, lps, dev_bytes, f32 = run(np.float32)
     pts = float(sum(n * n for n, _, _ in cases))
     m0 = [float(c0.sum()) for _, _, c0 in cases]
+    # solves whose diffusive eigenvalue dt*kappa*|k|^2_max lies beyond RK4's
+    # real-axis stability limit: they diverge in any precision (the FP64
+    # oracle included) and are left out of the accuracy statistics
+    unstable = [i for i, (n, κ, _) in enumerate(cases) if 0.005 * κ * 2 * (n / 2) ** 2 > RK4_REAL_AXIS_LIMIT]
+    ok = [i for i in range(len(cases)) if i not in unstable]
     res = {"solves": len(cases), "sizes": {str(k): int((sizes == k).sum()) for k in (64, 128, 256, 512)},
            "steps": steps, "ms_per_step": ms / steps, "grid_pt_steps_per_s": pts * steps / (ms / 1e3),
            "setup_s": setup, "launches_per_step": lps, "device_bytes": dev_bytes,
-           "mass_drift_fp32_max_abs": max(abs(_drift(c, m)) for c, m in zip(f32, m0)),
+           "rk4_unstable_solves": {"count": len(unstable), "criterion": "dt*kappa*|k|^2_max > 2.785 (RK4 real-axis "
+                                   "limit) at dt=0.005: 512^2 solves with kappa > 4.2e-3; they diverge in every "
+                                   "precision and are excluded from the accuracy figures",
+                                   "diverged_fp32": int(sum(not _bounded(f32[i], cases[i][2]) for i in unstable))},
+           "stable_solves_bounded_fp32": int(sum(_bounded(f32[i], cases[i][2]) for i in ok)),
+           "mass_drift_fp32_max_abs": max(abs(_drift(f32[i], m0[i])) for i in ok),
            "workload": f"256 solves n in {{64..512}}, RK4 dt=0.005, {steps} steps, cellular psi=cos(x+0.3 sin t)cos y at "
                        f"{'stage times' if time_mode == 'stage' else 'clock.t (frozen per step)'}, FP32 with FP64 k=0 mode"}
     if fp64_check:
         ms64, _, _, _, f64 = run(np.float64)
-        rel = [_rel(a, b) for a, b in zip(f32, f64)]
-        dd = [abs(_drift(a, m) - _drift(b, m)) for a, b, m in zip(f32, f64, m0)]
-        res["fp64_batched"] = {"ms_per_step": ms64 / steps, "grid_pt_steps_per_s": pts * steps / (ms64 / 1e3)}
-        res["rel_l2_fp32_vs_fp64_gpu"] = {"max": max(rel), "median": float(np.median(rel)),
+        rel = [_rel(f32[i], f64[i]) for i in ok]
+        dd = [abs(_drift(f32[i], m0[i]) - _drift(f64[i], m0[i])) for i in ok]
+        res["fp64_batched"] = {"ms_per_step": ms64 / steps, "grid_pt_steps_per_s": pts * steps / (ms64 / 1e3),
+                               "stable_solves_bounded": int(sum(_bounded(f64[i], cases[i][2]) for i in ok)),
+                               "unstable_solves_diverged": int(sum(not _bounded(f64[i], cases[i][2])
+                                                                   for i in unstable))}
+        res["rel_l2_fp32_vs_fp64_gpu"] = {"solves": len(rel), "max": max(rel), "median": float(np.median(rel)),
                                           "solves_over_1e-5": int(sum(r > 1e-5 for r in rel))}
         res["mass_drift_fp32_minus_fp64_max_abs"] = max(dd)
-        res["mass_drift_fp64_max_abs"] = max(abs(_drift(c, m)) for c, m in zip(f64, m0))
+        res["mass_drift_fp64_max_abs"] = max(abs(_drift(f64[i], m0[i])) for i in ok)
     if oracle_solves:
         o = oracle_module()
         picks = sorted([i for i, (n, _, _) in enumerate(cases) if n == 64], key=lambda i: cases[i][1])[:oracle_solves]
@@ -932,10 +971,19 @@ def run_served_stream(pkg, T, nreq, rate, seed=5150, pool=8, check=8, max_queued
     srv.wait_all(7200)
     wall = time.perf_counter() - t0
     st = srv.stats()
-    drifts = [srv.result_info(i)["mass_drift"] for i in ids]
+    drifts, diverged = [], []
+    for i, rid in enumerate(ids):
+        _, c = srv.poll(rid)
+        if _bounded(c, inputs(reqs[i])[1]):
+            drifts.append(srv.result_info(rid)["mass_drift"])
+        else:
+            three, n, nsteps, κ, dt, _, _, _ = reqs[i]
+            diverged.append({"dim": 3 if three else 2, "n": n, "steps": nsteps, "kappa": κ, "dt": dt})
     chk = {}
+    diverged_keys = {(d["n"], d["steps"], d["kappa"]) for d in diverged}
     if check:
-        picks = [i for i in range(nreq) if reqs[i][1] <= 256 and not reqs[i][0]][:check]
+        picks = [i for i in range(nreq) if reqs[i][1] <= 256 and not reqs[i][0]
+                 and (reqs[i][1], reqs[i][2], reqs[i][3]) not in diverged_keys][:check]  # bounded requests only
         errs, dd = [], []
         for i in picks:
             spec, c0, (u, v) = inputs(reqs[i])
@@ -950,9 +998,24 @@ def run_served_stream(pkg, T, nreq, rate, seed=5150, pool=8, check=8, max_queued
             m0 = float(c0.sum())
             dd.append(abs(_drift(c, m0) - _drift(p.vars.c, m0)))
             del p
-        chk = {"requests": len(picks), "what": "result vs the same request run alone by an FP64 single-solve handle",
+        # the smallest diverged 2D request, run by the FP64 CPU oracle: it diverges there too
+        small = sorted([i for i in range(nreq) if not reqs[i][0] and reqs[i][1] <= 128
+                        and (reqs[i][1], reqs[i][2], reqs[i][3]) in diverged_keys],
+                       key=lambda i: reqs[i][1] * reqs[i][2])
+        if small:
+            i = small[0]
+            spec, c0, (u, v) = inputs(reqs[i])
+            o = oracle_module()
+            r = o.Problem(o.TwoDAdvectingFlow(u=lambda *a: u, v=lambda *a: v), nx=spec.n, kappa=spec.kappa,
+                          dt=spec.dt)
+            o.set_c(r, c0)
+            o.stepforward(r, spec.nsteps)
+            o.updatevars(r)
+            chk["oracle_on_a_diverged_request"] = {"n": spec.n, "steps": spec.nsteps, "kappa": spec.kappa,
+                                                   "oracle_bounded": _bounded(r.vars.c, c0)}
+        chk.update({"requests": len(picks), "what": "result vs the same request run alone by an FP64 single-solve handle",
                "rel_l2_max": max(errs) if errs else None, "rel_l2_median": float(np.median(errs)) if errs else None,
-               "mass_drift_diff_max_abs": max(dd) if dd else None}
+               "mass_drift_diff_max_abs": max(dd) if dd else None})
     srv.close()
     work = sum(r[1] ** (3 if r[0] else 2) * r[2] for r in reqs)
     return {"requests": nreq, "arrival_rate_per_s": rate, "completed": st["completed"], "failed": st["failed"],
@@ -960,6 +1023,11 @@ def run_served_stream(pkg, T, nreq, rate, seed=5150, pool=8, check=8, max_queued
             "grid_pt_steps_per_s": st["grid_point_steps"] / wall, "wall_s": wall, "total_grid_pt_steps": work,
             "peak_device_bytes": st["device_bytes"], "input_prep_s": prep, "feeder_holds": holds[0],
             "mass_drift_max_abs": max(abs(d) for d in drifts), "mass_drift_median_abs": float(np.median(np.abs(drifts))),
+            "diverged": {"count": len(diverged), "examples": diverged[:6],
+                         "why": "under-resolved: the advective form, like the reference's, is not dealiased; "
+                                "at kappa near 1e-4 on small grids the tracer is thinned below the grid scale "
+                                "and the aliasing instability grows in every precision (mass drift and the "
+                                "FP64 check are over the bounded results)"},
             "fp64_check": chk,
             "mix": "2D n in {64..1024} (90%), 3D 128^3 (10%); steps log-uniform [100,5000]; kappa log-uniform "
                    f"[1e-4,1e-2]; RK4; flows from a seeded pool of {pool} per size"}
@@ -999,10 +1067,28 @@ def run_profile_case(args):
                       "warmup": args.warmup, "steps": args.steps, "tuning": p.tuning}), flush=True)
 
 
+def run_workloads_only(args):
+    """Only the secondary configurations (for instance the full 10,000-request
+    served stream: --workloads-only --only served_fp32 --serve-requests 10000),
+    printed as one JSON line; not the contract's bench line."""
+    import torch
+    import __graft_entry__ as g
+    if not (g.PKG_DIR / "libptf.so").exists():
+        g.build()
+    pkg = g.load_package()
+    torch.cuda.set_device(0)
+    sampler = ClockSampler(torch.cuda.current_device())
+    sampler.start()
+    w = run_workloads(args, pkg, torch)
+    print(json.dumps({"workloads_only": True, "workloads": w, "clocks": sampler.stop()}), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workloads_only:
+        run_workloads_only(args)
     elif args.profile_case:
         run_profile_case(args)
     else:

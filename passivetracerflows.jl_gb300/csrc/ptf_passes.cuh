@@ -129,14 +129,19 @@ __device__ __forceinline__ T kval(int p, T dk) { return (T)(p < N / 2 ? p : p - 
 // Consecutive threads therefore touch consecutive columns: a warp reads
 // W-element segments.  MODE is a compile-time ColMode.
 // ---------------------------------------------------------------------------
+// FP32 column blocks: up to 512 threads at 128 registers each -- two blocks
+// of 256 threads (4 columns of 1024) or one of 512 (8 columns: 64-byte row
+// segments, which DRAM serves markedly better than 32-byte ones; measured 5%
+// faster per 1024-point column launch, and 2 instead of 1 column per block
+// at 4096).  The register budget is the same for both shapes; the tuner picks.
 #ifndef PTF_COL_MINB_F32
-#define PTF_COL_MINB_F32 2
+#define PTF_COL_MINB_F32 1
 #endif
 #ifndef PTF_COL_MINB_F64
 #define PTF_COL_MINB_F64 1
 #endif
 #ifndef PTF_COL_THREADS_F32
-#define PTF_COL_THREADS_F32 256
+#define PTF_COL_THREADS_F32 512
 #endif
 #ifndef PTF_EARLY_OPERAND
 #define PTF_EARLY_OPERAND 1  // fetch a stage operand ahead with cp.async (see col_body)
