@@ -19,6 +19,7 @@
 #include <cstddef>
 #include <complex>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -113,6 +114,8 @@ struct ptf_handle {
   ptf_config cfg;
   int dim = 2, nx = 0, ny = 0, nz = 1;
   int nkr = 0, pitch = 0;
+  int ylog = 0;             // spectral layout: rows interleaved in groups of 2^ylog (spec_index)
+  int priv = 0;             // 1: state and tables in the main column pass's register order (SpecMap)
   long long plane = 0;      // spectral elements per solve (nz*ny*pitch)
   long long nphys = 0;      // physical points per solve (nz*ny*nx)
   long long rows = 0;       // x rows per solve (nz*ny)
@@ -200,6 +203,28 @@ template <typename T> void fill_twiddles(std::vector<T>& out, int n) {
 size_t elem_c(const ptf_handle* h) { return h->fp32 ? sizeof(float2) : sizeof(double2); }
 size_t elem_r(const ptf_handle* h) { return h->fp32 ? sizeof(float) : sizeof(double); }
 
+// Layouts of a handle's fields: intermediates (A, B, C, Nx) in the
+// interleaved spectral layout; the state (s, si, acc) and the tables in the
+// main column pass's register order when h->priv (SpecMap).
+SpecMap lay_map(const ptf_handle* h) {
+  SpecMap m;
+  m.pitch = h->pitch;
+  m.ylog = h->ylog;
+  return m;
+}
+SpecMap state_map(const ptf_handle* h) {
+  SpecMap m = lay_map(h);
+  if (!h->priv) return m;
+  m.priv = 1;
+  m.n = h->gmain.n;
+  if (h->fp32) col_line_shape<float>(m.n, &m.tpl, &m.rf);
+  else col_line_shape<double>(m.n, &m.tpl, &m.rf);
+  m.pl = h->fp32 ? 2 : 1;
+  m.ny = h->ny;
+  m.three = h->dim == 3;
+  return m;
+}
+
 template <typename T> int upload(ptf_handle* h, void* dst, const std::vector<T>& src, const char* what) {
   cudaError_t e = cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -208,10 +233,13 @@ template <typename T> int upload(ptf_handle* h, void* dst, const std::vector<T>&
 }
 
 // L (src/traceradvectiondiffusion.jl:538-554) and, for ETDRK4, its six
-// coefficient planes, one value per spectral element [nz][ny][pitch].
+// coefficient planes, one value per spectral element in the layout of the
+// state (state_map over the rows q * ny + j).
 template <typename T> int upload_tables(ptf_handle* h) {
   const ptf_config& c = h->cfg;
-  const int ny = h->ny, nz = h->nz, pitch = h->pitch, nkr = h->nkr;
+  const int ny = h->ny, nz = h->nz, nkr = h->nkr;
+  const SpecMap sm = state_map(h);
+  auto at = [&](int q, int j, int k) { return (size_t)spec_map(sm, (long long)q * ny + j, k); };
   const double dkx = 2 * M_PI / c.Lx, dky = h->dim >= 2 ? 2 * M_PI / c.Ly : 0.0, dkz = h->dim == 3 ? 2 * M_PI / c.Lz : 0.0;
   const size_t plane = (size_t)h->plane;
   std::vector<double> L(plane, 0.0);
@@ -226,7 +254,7 @@ template <typename T> int upload_tables(ptf_handle* h) {
         if (c.kappah != 0.0) hyp = c.kappah * std::pow(krsq, (double)c.nkappah);
         double Lv = -c.kappa * kr * kr - c.eta * l * l - hyp;
         if (h->dim == 3) Lv -= c.iota * m * m;
-        L[((size_t)q * ny + j) * pitch + k] = Lv;
+        L[at(q, j, k)] = Lv;
       }
     }
   }
@@ -258,7 +286,7 @@ template <typename T> int upload_tables(ptf_handle* h) {
         for (int k = 0; k < nkr; ++k) {
           const double a = k * dkx * dx / M_PI, b = l * dy / M_PI, e = m * dz / M_PI;
           const double K = std::sqrt(a * a + b * b + e * e);
-          ft[((size_t)q * ny + j) * pitch + k] = (T)(K < innerK ? 1.0 : std::exp(-decay * std::pow(K - innerK, order)));
+          ft[at(q, j, k)] = (T)(K < innerK ? 1.0 : std::exp(-decay * std::pow(K - innerK, order)));
         }
       }
     }
@@ -275,7 +303,7 @@ template <typename T> int upload_tables(ptf_handle* h) {
       const int k = (int)(idx % nkr);
       const int j = (int)((idx / nkr) % (ny / 2 + 1));
       const int q = (int)(idx / ((long long)nkr * (ny / 2 + 1)));
-      const double Lv = L[((size_t)q * ny + j) * pitch + k];
+      const double Lv = L[at(q, j, k)];
       double ph[4];
       etd_phis(dt * Lv, ph);
       // E - 1 and E2 - 1 (expm1): the stage combination applies s + (E - 1) s
@@ -285,7 +313,7 @@ template <typename T> int upload_tables(ptf_handle* h) {
       const int qs[2] = {q, (nz - q) % nz};
       for (int a = 0; a < 2; ++a)
         for (int b = 0; b < (h->dim == 3 ? 2 : 1); ++b)
-          for (int e = 0; e < 6; ++e) cf[e * plane + ((size_t)qs[b] * ny + js[a]) * pitch + k] = (T)vals[e];
+          for (int e = 0; e < 6; ++e) cf[e * plane + at(qs[b], js[a], k)] = (T)vals[e];
     });
     rc = upload(h, h->coef, cf, "upload ETDRK4 coefficients");
     if (rc) return rc;
@@ -408,6 +436,10 @@ template <typename T> int run_col(ptf_handle* h, const ColGeom& g, int mode, con
   a.dt = (T)h->cfg.dt;
   a.dk = (T)g.dk;
   a.stride = g.stride; a.mode = mode; a.do_inverse = do_inverse ? 1 : 0;
+  // lines along y run over the interleaved rows; the 3D z lines over flat
+  // in-plane offsets, which any layout leaves contiguous
+  a.ylog = g.axis == 1 ? h->ylog : 0;
+  a.priv = (&g == &h->gmain) ? h->priv : 0;  // the state and tables are the main pass's
   a.bstride = g.bstride; a.tplane = h->plane; a.tab_per_block = 0;
   if (h->k0mode && &g == &h->gmain) {
     a.k0 = h->k0 + 4 * (size_t)gr.b0;
@@ -444,7 +476,7 @@ int run_row(ptf_handle* h, int mode, const void* A, const void* B, const void* C
   a.tw = (const C*)h->twx;
   a.dkx = (T)(2 * M_PI / h->cfg.Lx);
   a.scale = (T)scale;
-  a.rows = (int)h->rows; a.pitch = h->pitch; a.mode = mode;
+  a.rows = (int)h->rows; a.pitch = h->pitch; a.mode = mode; a.ylog = h->ylog;
   a.park_slots = h->dim == 3 ? 2 : 1;
   a.err = h->err_dev;
   a.tma = (h->row_tma && h->dim == 2 && mode == ROW_RHS) ? 1 : 0;
@@ -772,7 +804,7 @@ int check_where(ptf_handle* h, int32_t where) {
   return PTF_OK;
 }
 
-int spec_in(ptf_handle* h, const double* sol, int32_t where, void* dst) {
+int spec_in(ptf_handle* h, const double* sol, int32_t where, void* dst, const SpecMap& map) {
   const long long rows = h->rows * h->cfg.batch;
   const long long n = rows * h->nkr;
   const double2* src = (const double2*)sol;
@@ -782,20 +814,20 @@ int spec_in(ptf_handle* h, const double* sol, int32_t where, void* dst) {
     if (e != cudaSuccess) return cuda_fail(h, e, "spectral copy");
     src = (const double2*)h->stage;
   }
-  e = h->fp32 ? launch_spec_in<float>(src, (float2*)dst, h->nkr, h->pitch, rows, h->stream)
-              : launch_spec_in<double>(src, (double2*)dst, h->nkr, h->pitch, rows, h->stream);
+  e = h->fp32 ? launch_spec_in<float>(src, (float2*)dst, h->nkr, h->pitch, rows, h->stream, &map, h->rows)
+              : launch_spec_in<double>(src, (double2*)dst, h->nkr, h->pitch, rows, h->stream, &map, h->rows);
   h->launches++;
   if (e != cudaSuccess) return cuda_fail(h, e, "spectral convert");
   return PTF_OK;
 }
 
 // k0patch: the (0,0[,0]) element of each solve comes from the FP64 k = 0 state
-int spec_out(ptf_handle* h, const void* src, double* user, int32_t where, bool k0patch = false) {
+int spec_out(ptf_handle* h, const void* src, double* user, int32_t where, const SpecMap& map, bool k0patch = false) {
   const long long rows = h->rows * h->cfg.batch;
   const long long n = rows * h->nkr;
   double2* dst = (where == PTF_HOST) ? (double2*)h->stage : (double2*)user;
-  cudaError_t e = h->fp32 ? launch_spec_out<float>((const float2*)src, dst, h->nkr, h->pitch, rows, h->stream)
-                          : launch_spec_out<double>((const double2*)src, dst, h->nkr, h->pitch, rows, h->stream);
+  cudaError_t e = h->fp32 ? launch_spec_out<float>((const float2*)src, dst, h->nkr, h->pitch, rows, h->stream, &map, h->rows)
+                          : launch_spec_out<double>((const double2*)src, dst, h->nkr, h->pitch, rows, h->stream, &map, h->rows);
   h->launches++;
   if (e == cudaSuccess && k0patch) {
     e = launch_k0_to_spec(dst, h->rows * h->nkr, h->cfg.batch, h->k0, h->stream);
@@ -867,7 +899,7 @@ int apply_tuning(ptf_handle* h, const ptf_tuning& t) {
   h->rowP = t.row_pairs;
   h->branches = t.branches;
   h->group = t.solves_per_group;
-  h->row_tma = h->dim == 2 ? t.row_staged : 0;
+  h->row_tma = (h->dim == 2 && h->ylog == 0) ? t.row_staged : 0;
   h->tuned_ms = t.ms_per_step;
   drop_graph(h);
   return PTF_OK;
@@ -933,7 +965,7 @@ template <typename T> int autotune_impl(ptf_handle* h, int steps) {
       else if (knob == 1) { if (h->dim != 3 || !lines_ok(h, h->gy3.n, true, v, h->gy3.ncols)) continue; t.col_lines_y = v; }
       else if (knob == 2) { if (!lines_ok(h, h->nx, false, v, row_pairs_total(h))) continue; t.row_pairs = v; }
       else if (knob == 3) { if (v > 4 || v > h->cfg.batch || h->dim == 1) continue; t.branches = v; t.solves_per_group = 0; }
-      else { if (v > 2 || h->dim != 2) continue; t.row_staged = v - 1; }
+      else { if (v > 2 || h->dim != 2 || h->ylog != 0) continue; t.row_staged = v - 1; }
       cands.push_back(t);
     }
     for (const ptf_tuning& t : cands) {
@@ -1035,6 +1067,18 @@ int ptf_create(const ptf_config* cfg, ptf_handle** out) {
   h->plane = (long long)h->nz * h->ny * h->pitch;
   h->nphys = (long long)h->nz * h->ny * h->nx;
   h->rows = (long long)h->nz * h->ny;
+  // spectral layout: rows in groups of four where the y lines allow (1D: plain).
+  // PTF_SPEC_YLOG (0..2) caps it, for comparing layouts.
+  if (h->dim >= 2) {
+    h->ylog = h->fp32 ? col_ylog_limit<float>(h->ny) : col_ylog_limit<double>(h->ny);
+    if (const char* ev = std::getenv("PTF_SPEC_YLOG")) {
+      const int cap = std::atoi(ev);
+      if (cap >= 0 && cap < h->ylog) h->ylog = cap;
+    }
+    // the state and tables in the main pass's register order (PTF_SPEC_PRIV=0: off)
+    const char* ev = std::getenv("PTF_SPEC_PRIV");
+    h->priv = (ev && std::atoi(ev) == 0) ? 0 : 1;
+  }
   cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { ptf_destroy(h); return cuda_fail(nullptr, e, "stream create"); }
   h->own_stream = true;
@@ -1214,14 +1258,14 @@ int ptf_get_sol(ptf_handle* h, double* sol, int32_t where) {
   if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
   if (!sol) return fail(h, PTF_ERR_ARG, "null field");
   if (check_where(h, where)) return PTF_ERR_ARG;
-  return spec_out(h, h->s, sol, where, h->k0mode);
+  return spec_out(h, h->s, sol, where, state_map(h), h->k0mode);
 }
 
 int ptf_set_sol(ptf_handle* h, const double* sol, int32_t where) {
   if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
   if (!sol) return fail(h, PTF_ERR_ARG, "null field");
   if (check_where(h, where)) return PTF_ERR_ARG;
-  int rc = spec_in(h, sol, where, h->s);
+  int rc = spec_in(h, sol, where, h->s, state_map(h));
   if (rc) return rc;
   if (h->k0mode) {
     const double2* src = where == PTF_HOST ? (const double2*)h->stage : (const double2*)sol;
@@ -1261,10 +1305,10 @@ int ptf_calcN(ptf_handle* h, const double* sol, double* N, int32_t where) {
     cudaError_t e = h->fp32 ? eval_flow<float>(h, h->t) : eval_flow<double>(h, h->t);
     if (e != cudaSuccess) return cuda_fail(h, e, "flow evaluation");
   }
-  int rc = spec_in(h, sol, where, sbuf);
+  int rc = spec_in(h, sol, where, sbuf, state_map(h));  // read as a state by the prologue
   if (!rc) rc = h->fp32 ? calcN_impl<float>(h, sbuf) : calcN_impl<double>(h, sbuf);
   if (rc) return rc;
-  return spec_out(h, sbuf, N, where);
+  return spec_out(h, sbuf, N, where, lay_map(h));  // the forward pass writes an intermediate
 }
 
 int ptf_clock(const ptf_handle* h, double* t, int64_t* step) {

@@ -29,6 +29,11 @@ template <typename T> cudaError_t launch_row(int nx, const RowArgs<T>& a, int P,
 template <typename T> int max_lines_per_block(int n, bool col);
 // Default W (col) or P (row) for length n; `divisor` must be divisible by it.
 template <typename T> int default_lines_per_block(int n, bool col, int divisor);
+// Largest spectral layout (ylog of spec_index) a column pass of length n takes.
+template <typename T> int col_ylog_limit(int n);
+// Threads per line and last forward radix of a column pass of length n
+// (the register order of SpecMap).
+template <typename T> void col_line_shape(int n, int* tpl, int* rf);
 
 // 1D stage passes (ptf_kern1d.cu): nblk blocks of P solve pairs; mode is a
 // stepper stage (COL_RK4_*, COL_ETD_*) or COL_FWD_N (N into xout).
@@ -39,9 +44,15 @@ template <typename T> int line1d_tpl(int nx);  // threads per solve pair
 // Element conversions (ptf_util.cu).
 template <typename T> cudaError_t launch_real_in(const double* src, T* dst, long long n, double scale, cudaStream_t st);
 template <typename T> cudaError_t launch_real_out(const T* src, double* dst, long long n, cudaStream_t st);
-// user spectral layout (nkr complex per row) <-> pitched internal layout
-template <typename T> cudaError_t launch_spec_in(const double2* src, typename cplx_of<T>::type* dst, int nkr, int pitch, long long rows, cudaStream_t st);
-template <typename T> cudaError_t launch_spec_out(const typename cplx_of<T>::type* src, double2* dst, int nkr, int pitch, long long rows, cudaStream_t st);
+// user spectral layout (nkr complex per row) <-> pitched internal layout:
+// the plain [rows][pitch] layout without a map, else spec_map(*map, r, k)
+// within each solve of rows_per_solve rows
+template <typename T>
+cudaError_t launch_spec_in(const double2* src, typename cplx_of<T>::type* dst, int nkr, int pitch, long long rows,
+                           cudaStream_t st, const SpecMap* map = nullptr, long long rows_per_solve = 0);
+template <typename T>
+cudaError_t launch_spec_out(const typename cplx_of<T>::type* src, double2* dst, int nkr, int pitch, long long rows,
+                            cudaStream_t st, const SpecMap* map = nullptr, long long rows_per_solve = 0);
 
 // FP64 k = 0 mode (ptf_util.cu).  Per-solve sums of x (n values per solve):
 // out[b * out_stride]; partials holds 64 doubles per solve.

@@ -68,6 +68,28 @@ template <typename T> int default_lines_per_block(int n, bool col, int divisor) 
   return m < 1 ? 1 : m;
 }
 
+template <typename T> int col_ylog_limit(int n) {
+  switch (n) {
+#define PTF_CASE(v) case v: return col_ylog_max<T, v>();
+    PTF_FOR_SIZES(PTF_CASE)
+#undef PTF_CASE
+    default: return 0;
+  }
+}
+
+template <typename T> void col_line_shape(int n, int* tpl, int* rf) {
+  switch (n) {
+#define PTF_CASE(v) case v: *tpl = col_tpl<T, v>(); *rf = LastRadix<v, -1, ColE<T, v>::value>::value; return;
+    PTF_FOR_SIZES(PTF_CASE)
+#undef PTF_CASE
+    default: *tpl = 1; *rf = 1;
+  }
+}
+
+template void col_line_shape<float>(int, int*, int*);
+template void col_line_shape<double>(int, int*, int*);
+template int col_ylog_limit<float>(int);
+template int col_ylog_limit<double>(int);
 template cudaError_t launch_col<float>(int, const ColArgs<float>&, int, int, int, cudaStream_t, int);
 template cudaError_t launch_col<double>(int, const ColArgs<double>&, int, int, int, cudaStream_t, int);
 template cudaError_t launch_row<float>(int, const RowArgs<float>&, int, int, int, cudaStream_t);

@@ -42,6 +42,8 @@ template <typename T, int N> struct PassLaunch {
     return col_k<MODE, 0>(a, W, nbx, batch, st, carve);
   }
   static cudaError_t col(const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st, int carve = -1) {
+    // the layout's row groups must divide every register's row offset
+    if (a.ylog < 0 || a.ylog > col_ylog_max<T, N>()) return cudaErrorInvalidValue;
     switch (a.mode) {
       case COL_PROLOGUE: return col_m<COL_PROLOGUE>(a, W, nbx, batch, st, carve);
       case COL_FWD_STORE: return col_m<COL_FWD_STORE>(a, W, nbx, batch, st, carve);
@@ -59,8 +61,10 @@ template <typename T, int N> struct PassLaunch {
     }
   }
   static cudaError_t row(const RowArgs<T>& a, int P, int nby, int batch, cudaStream_t st) {
-    // the staged variant when its shared memory fits, else the direct kernel
-    if (a.tma && a.mode == ROW_RHS && row_tma_smem_bytes<T, N>(P, a.pitch) <= 227u * 1024u &&
+    // the staged variant (plain layout only) when its shared memory fits,
+    // else the direct kernel
+    if (a.ylog < 0 || a.ylog > 2) return cudaErrorInvalidValue;
+    if (a.tma && a.ylog == 0 && a.mode == ROW_RHS && row_tma_smem_bytes<T, N>(P, a.pitch) <= 227u * 1024u &&
         P * pass_tpl<T, N>() <= max_threads(row_rhs_tma_kernel<T, N>)) {
       const size_t smem = row_tma_smem_bytes<T, N>(P, a.pitch);
       cudaError_t e = cudaFuncSetAttribute(row_rhs_tma_kernel<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -69,11 +73,16 @@ template <typename T, int N> struct PassLaunch {
       row_rhs_tma_kernel<T, N><<<dim3(nby, batch), dim3(P * pass_tpl<T, N>()), smem, st>>>(a);
       return cudaGetLastError();
     }
-    if (P * pass_tpl<T, N>() > max_threads(row_pass_kernel<T, N>)) return cudaErrorInvalidConfiguration;
+    return a.ylog > 0 ? row_k<true>(a, P, nby, batch, st) : row_k<false>(a, P, nby, batch, st);
+  }
+  // rows of a pair interleaved (PAIRED: spectral layout ylog >= 1) or not
+  template <bool PAIRED> static cudaError_t row_k(const RowArgs<T>& a, int P, int nby, int batch, cudaStream_t st) {
+    auto kern = row_pass_kernel<T, N, PAIRED>;
+    if (P * pass_tpl<T, N>() > max_threads(kern)) return cudaErrorInvalidConfiguration;
     const size_t smem = row_smem_bytes<T, N>(P, a.park_slots < 1 ? 1 : a.park_slots);
-    cudaError_t e = cudaFuncSetAttribute(row_pass_kernel<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    row_pass_kernel<T, N><<<dim3(nby, batch), dim3(P * pass_tpl<T, N>()), smem, st>>>(a);
+    kern<<<dim3(nby, batch), dim3(P * pass_tpl<T, N>()), smem, st>>>(a);
     return cudaGetLastError();
   }
 };

@@ -1,7 +1,8 @@
 // Pass kernels of the tracer advection-diffusion right-hand side (2D and 3D).
 //
 // Spectral arrays are [nz][ny][pitch] complex with kr fastest (the layout of
-// the reference's (nkr, nl[, nm]) column-major arrays, padded to `pitch`);
+// the reference's (nkr, nl[, nm]) column-major arrays, padded to `pitch`),
+// rows interleaved in small groups (spec_index below);
 // physical arrays are [nz][ny][nx] real, x fastest (nz = 1 in 2D).  One RHS
 // evaluation (calcN!, src/traceradvectiondiffusion.jl:756-786) is split into
 // passes along one axis each:
@@ -11,11 +12,11 @@
 //       operator, then the inverse FFTs of the next stage input s and of
 //       i*k_axis*s -> A, B.  The same kernel, in other modes, is the 3D
 //       y-forward pass and the 3D y-inverse pass (three outputs).
-//   row pass (x): per pair of rows, inverse x-FFT of Z = i(kr A + B)
-//       (Hermitian-extended; Re z = c_x, Im z = c_y; in 3D one more packed
-//       inverse gives c_z of both rows), the product n = -(u.grad c), and one
-//       forward x-FFT of n_y0 + i n_y1, separated into the two rows' half
-//       spectra.
+//   row pass (x): per pair of rows, one inverse x-FFT of the two rows' i kr A
+//       (Hermitian-extended, packed as row 0 + i row 1) gives c_x of both
+//       rows, one of B gives c_y (in 3D one of C gives c_z), then the
+//       products n = -(u.grad c) of the two rows form one forward x-FFT of
+//       n_y0 + i n_y1, separated into the two rows' half spectra.
 //
 // The flow passed to the row pass is pre-scaled by -1/(2 N) (N = grid
 // points): that folds the inverse normalisation, the minus sign and the 1/2
@@ -38,6 +39,47 @@ constexpr int COL_NMODES = 12;
 enum RowMode : int { ROW_RHS = 0, ROW_C2R = 1, ROW_R2C = 2, ROW_RHS3 = 3 };
 
 enum FlowKind : int { FLOW_ARRAYS = 0, FLOW_CELLULAR = 1 };
+
+// Spectral layout.  A field is `rows` (the flat (z, y) index) by `pitch`
+// complex values, its rows interleaved in groups of 2^ylog: element (r, k)
+// sits at (((r >> ylog) * pitch + k) << ylog) + (r & (2^ylog - 1)).  ylog = 0
+// is the plain [rows][pitch] layout.  With ylog >= 1 the two rows of a row
+// pair are adjacent (one 16-byte access serves both in FP32), and a column
+// pass block of W columns moves runs of W * 2^ylog values instead of W.
+__host__ __device__ __forceinline__ long long spec_row_base(long long r, int pitch, int ylog) {
+  return (((r >> ylog) * (long long)pitch) << ylog) + (r & ((1LL << ylog) - 1));
+}
+__host__ __device__ __forceinline__ long long spec_index(long long r, long long k, int pitch, int ylog) {
+  return spec_row_base(r, pitch, ylog) + (k << ylog);
+}
+
+// Register order.  The fields only the main column pass touches -- the
+// stepper state (sol, stage input, accumulator) and the tables (L, ETDRK4
+// coefficients, filter) -- are stored in the order the pass holds them:
+// for column c (2D: kr; 3D: the in-plane offset) and position p along the
+// line, held by thread t in register i (p = t + (i / RF) TPL + (i % RF) n / RF,
+// the last forward stage's pattern), at (((c >> pl) n + i TPL + t) << pl) +
+// (c & (2^pl - 1)).  A warp's access of one register is then one contiguous
+// run, whatever the columns per block.  pl = 2 in FP32, 1 in FP64.
+struct SpecMap {
+  int pitch = 0, ylog = 0;      // rows interleaved in groups of 2^ylog (spec_index)
+  int priv = 0;                 // 1: register order of the main column pass
+  int n = 0, tpl = 0, rf = 0;   // main pass: line length, threads per line, last forward radix
+  int pl = 0;                   // log2 columns per register-order group
+  int ny = 0, three = 0;        // 3D: the main pass runs along z over planes of ny rows
+};
+__host__ __device__ __forceinline__ long long priv_index(const SpecMap& m, long long p, long long c) {
+  const int t = (int)(p % m.tpl);
+  const int rest = (int)(p - t), nr = m.n / m.rf;
+  const int i = ((rest % nr) / m.tpl) * m.rf + rest / nr;
+  return ((((c >> m.pl) * m.n) + (long long)i * m.tpl + t) << m.pl) + (c & ((1LL << m.pl) - 1));
+}
+// Element (row r of a solve, bin k) under map m.
+__host__ __device__ __forceinline__ long long spec_map(const SpecMap& m, long long r, long long k) {
+  if (!m.priv) return spec_index(r, k, m.pitch, m.ylog);
+  if (m.three) return priv_index(m, r / m.ny, spec_index(r % m.ny, k, m.pitch, m.ylog));
+  return priv_index(m, r, k);
+}
 
 // Per-solve parameters of the batched form (one entry per slot of a bucket
 // of equally sized square 2D solves).  The clock (t, step) advances on the
@@ -71,7 +113,9 @@ template <typename T> struct ColArgs {
   const T* Ltab;   // linear operator, one value per spectral element
   const T* coef;   // ETDRK4 tables E, E2, zeta, alpha, beta, gamma, `tplane` apart
   T dt, dk;        // dk: 2*pi/L of the transform axis
-  int stride;      // elements between consecutive points of a line
+  int stride;      // elements between consecutive points of a line (the row pitch when ylog > 0)
+  int ylog;        // spectral layout (spec_index): lines along the interleaved row axis
+  int priv;        // 1: s, si, acc and the tables are in register order (SpecMap)
   int mode, do_inverse;
   long long bstride;    // elements between blockIdx.y blocks of fields
   long long tplane;     // elements of one table plane
@@ -105,6 +149,7 @@ template <typename T> struct RowArgs {
   const C* tw;     // NX-point twiddles
   T dkx, scale;    // scale: C2R normalisation / R2C 1/2 / RHS 1
   int rows, pitch, mode;
+  int ylog;        // spectral layout of A, B, Cin, out (spec_index)
   int park_slots;  // parking slots per point: 1 (2D) or 2 (3D)
   long long bstride, pstride, fstride;
   // batched form only
@@ -165,6 +210,12 @@ template <int N> struct ColE<float, N> { static constexpr int value = N >= 256 ?
 // threads per line: row pass (pass_tpl) and column pass (col_tpl)
 template <typename T, int N> __host__ __device__ constexpr int pass_tpl() { return N / PassE<T, N>::value; }
 template <typename T, int N> __host__ __device__ constexpr int col_tpl() { return N / ColE<T, N>::value; }
+// Largest spectral layout (ylog) a column pass of length N can address with
+// per-register row offsets (all multiples of col_tpl): 2 (rows in fours),
+// less for N < 64.
+template <typename T, int N> __host__ __device__ constexpr int col_ylog_max() {
+  return col_tpl<T, N>() >= 4 ? 2 : col_tpl<T, N>() >= 2 ? 1 : 0;
+}
 
 // Compensated FP64 sum of the real parts of column 0 of a column-pass block
 // (lines w = 0: threads t*W, registers v[0..E)), returned in thread 0.  Uses
@@ -393,9 +444,19 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
   C* line = sm + w * LS;
   C* park = sm + W * LS;  // slot i of this thread: park[i*blockDim + tid]
   const int nthr = blockDim.x;
-  const int tb = t * stride + col;  // this thread's offset inside one field
+  // this thread's offset inside one field: element (row t, column col) of
+  // the layout (spec_index); every register's row offset below is a multiple
+  // of TPL >= 2^ylog (the launcher checks), so it adds (offset * stride)
+  const int yl = a.ylog;
+  const int tb = (((t >> yl) * stride + col) << yl) + (t & ((1 << yl) - 1));
+  // register order of the private fields (SpecMap): column groups of 2^PL
+  constexpr int PL = sizeof(T) == 4 ? 2 : 1;
+  const bool priv = a.priv != 0;
+  const int pb = (((col >> PL) * N + t) << PL) + (col & ((1 << PL) - 1));
   // offset of register i for a first/last stage of radix R
 #define PTF_OFF(R, i) (tb + (((i) / (R)) * TPL + ((i) % (R)) * (N / (R))) * stride)
+  // a private field's register i (last forward stage pattern)
+#define PTF_POFF(i) (priv ? pb + (i) * (TPL << PL) : PTF_OFF(RF, i))
 
   constexpr bool K0MODE = (MODE >= COL_RK4_1 && MODE <= COL_ETD_4) || MODE == COL_FWD_STORE;
   const bool k0blk = !BATCHED && K0MODE && a.k0 != nullptr && tile == 0;  // uniform across the block
@@ -414,7 +475,7 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
   if (PF) {
     const C* __restrict__ op = (PF == 1 ? a.s : PF == 2 ? a.si : a.acc) + boff;
 #pragma unroll
-    for (int i = 0; i < E; ++i) cp_async<sizeof(C)>(park + i * nthr + threadIdx.x, op + PTF_OFF(RF, i));
+    for (int i = 0; i < E; ++i) cp_async<sizeof(C)>(park + i * nthr + threadIdx.x, op + PTF_POFF(i));
     cp_async_commit();
   }
   C v[E];
@@ -459,7 +520,7 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
     const T* __restrict__ cf = a.coef + 6 * toff;
 #pragma unroll
     for (int i = 0; i < E; ++i) {
-      const int o = PTF_OFF(RF, i);
+      const int o = PTF_POFF(i);  // the private fields (state, tables)
       const C Nh = v[i];  // forward transform of the RHS at this element
       C x;
       if (MODE == COL_PROLOGUE || MODE == COL_YINV3) {
@@ -467,7 +528,7 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
       } else if (MODE == COL_FWD_STORE) {
         x = Nh; if (store) S[o] = x;
       } else if (MODE == COL_FWD_N) {
-        x = Nh; if (store) a.nout[boff + o] = Nh;
+        x = Nh; if (store) a.nout[boff + PTF_OFF(RF, i)] = Nh;  // an intermediate: spectral layout
       } else {
         if (PF && i == 0) cp_async_wait_all();
         auto lf = [&]() { return Lval(Lt, o, i); };
@@ -534,6 +595,7 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
     for (int i = 0; i < E; ++i) Cp[PTF_OFF(RO, i)] = v[i];
   }
 #undef PTF_OFF
+#undef PTF_POFF
 }
 
 template <typename T, int N, int MODE, int CSTRIDE = 0>
@@ -576,25 +638,6 @@ __device__ __forceinline__ C zsrc_rhs(const C* Arow, const C* Brow, int k, int N
   }
   return z;
 }
-template <typename C>
-__device__ __forceinline__ C zsrc_c2r(const C* A0, const C* A1, int k, int NX) {
-  // Z[k] = P0[k] + i P1[k] with P0, P1 the Hermitian extensions of rows y0, y1.
-  C z;
-  const int h = NX / 2;
-  if (k == 0 || k == h) {
-    z.x = A0[k].x; z.y = A1[k].x;
-  } else if (k < h) {
-    const C p = A0[k], q = A1[k];
-    z.x = p.x - q.y; z.y = p.y + q.x;
-  } else {
-    const int kk = NX - k;
-    const C p = A0[kk], q = A1[kk];
-    // conj(p) + i conj(q)
-    z.x = p.x + q.y; z.y = -p.y + q.x;
-  }
-  return z;
-}
-
 // Shared memory of a row-pass block with P pairs: one FFT line and
 // `slots` parking slots per point of each pair (1 in 2D, 2 in 3D).
 template <typename T, int NX> __host__ __device__ constexpr size_t row_smem_bytes(int P, int slots) {
@@ -637,18 +680,76 @@ __device__ __forceinline__ CellularRow<T> cellular_row(const SlotParams<T>& sp, 
   r.Kx = sp.Kx;
   return r;
 }
+// The cellular flow at column x of a row pair (rows r0 = cr0, r1 = cr1 of
+// one slot): the x factor is shared by both rows.
 template <typename T, typename C>
-__device__ __forceinline__ void cellular_uv(const CellularRow<T>& r, const C* tw, int x, int n, T* u, T* v) {
-  const C e = grid_expi(tw, r.Kx, x, n);
-  const T ct = e.x * r.cphi - e.y * r.sphi, st = e.y * r.cphi + e.x * r.sphi;
-  *u = r.au * ct * r.sy;
-  *v = r.av * st * r.cy;
+__device__ __forceinline__ void cellular_uv2(const CellularRow<T>& r0, const CellularRow<T>& r1, const C* tw, int x,
+                                             int n, T* u0, T* v0, T* u1, T* v1) {
+  const C e = grid_expi(tw, r0.Kx, x, n);
+  const T ct = e.x * r0.cphi - e.y * r0.sphi, st = e.y * r0.cphi + e.x * r0.sphi;
+  *u0 = r0.au * ct * r0.sy;
+  *v0 = r0.av * st * r0.cy;
+  *u1 = r1.au * ct * r1.sy;
+  *v1 = r1.av * st * r1.cy;
+}
+
+// Input of an inverse x transform of two rows at once: Z[k] = H0[k] + i H1[k],
+// H_r the Hermitian extension of row r's half spectrum X_r = g Y_r with
+// g = i kr (DERIV) or 1, the imaginary parts at the self-conjugate bins
+// k = 0, NX/2 dropped (as a c2r transform does).  p, q = Y_0, Y_1 at
+// min(k, NX - k).  Re of the result is row 0's field, Im row 1's.
+template <bool DERIV, typename T, typename C>
+__device__ __forceinline__ C zpair(C p, C q, int k, int NX, T dkx) {
+  const int h = NX / 2;
+  if (DERIV) {
+    const T kr = (T)(k <= h ? k : NX - k) * dkx;
+    C a, b;
+    a.x = -kr * p.y; a.y = kr * p.x;
+    b.x = -kr * q.y; b.y = kr * q.x;
+    p = a; q = b;
+  }
+  C z;
+  if (k == 0 || k == h) {
+    z.x = p.x; z.y = q.x;
+  } else if (k < h) {
+    z.x = p.x - q.y; z.y = p.y + q.x;
+  } else {  // conj(p) + i conj(q)
+    z.x = p.x + q.y; z.y = q.x - p.y;
+  }
+  return z;
+}
+
+// Element `off` of both rows of a pair.  PAIRED: the rows are interleaved
+// (spectral layout ylog >= 1), row 1's element follows row 0's, and an FP32
+// pair is one 16-byte load.
+template <bool PAIRED, typename C>
+__device__ __forceinline__ void ld_pair(const C* __restrict__ r0, const C* __restrict__ r1, int off, C& x0, C& x1) {
+  if constexpr (PAIRED && sizeof(C) == 8) {
+    const float4 q = *reinterpret_cast<const float4*>(r0 + off);
+    x0.x = q.x; x0.y = q.y; x1.x = q.z; x1.y = q.w;
+  } else {
+    x0 = r0[off];
+    x1 = r1[off];
+  }
+}
+template <bool PAIRED, typename C>
+__device__ __forceinline__ void st_pair(C* r0, C* r1, int off, C x0, C x1) {
+  if constexpr (PAIRED && sizeof(C) == 8) {
+    *reinterpret_cast<float4*>(r0 + off) = make_float4(x0.x, x0.y, x1.x, x1.y);
+  } else {
+    r0[off] = x0;
+    r1[off] = x1;
+  }
 }
 
 // Body of one row-pass block (tile = pair tile index, blk = block of fields).
+// The rows of a pair are transformed together: one inverse x transform gives
+// c_x of both rows (Re, Im), a second c_y (and in 3D a third c_z), and the
+// products -(u.grad c) of the two rows form the one forward transform.
 // BATCHED: flat pairs run over the slots of a bucket; each thread carries
 // its slot, whose flow is an array or the analytic cellular flow.
-template <typename T, int NX, bool BATCHED>
+// PAIRED: the spectral layout interleaves rows (a.ylog >= 1).
+template <typename T, int NX, bool BATCHED, bool PAIRED = false>
 __device__ __forceinline__ void row_body(const RowArgs<T>& a, int tile, int blk, unsigned char* smem_raw) {
   typedef typename cplx_of<T>::type C;
   constexpr int E = PassE<T, NX>::value;
@@ -681,13 +782,17 @@ __device__ __forceinline__ void row_body(const RowArgs<T>& a, int tile, int blk,
     foff = (long long)slot * a.fstride;
   }
   const int pitch = a.pitch;
+  const int yl = PAIRED ? a.ylog : 0;
   C* line = sm + pr * LS;
   // this pair's parking slots: park[i*TPL + t] (and park[NX + i*TPL + t] in 3D)
   C* park = sm + P * LS + pr * a.park_slots * NX;
   const int yy0 = (BATCHED || valid) ? y0 : 0;
-  const long long r0 = boff + (long long)yy0 * pitch, r1 = r0 + pitch;
+  // the pair's rows in the spectral layout (row 1 follows row 0 when PAIRED)
+  const long long r0 = boff + spec_row_base(yy0, pitch, yl);
+  const long long r1 = PAIRED ? r0 + 1 : r0 + pitch;
   const long long q0 = (long long)yy0 * NX, q1 = q0 + NX;
-
+  constexpr int H = NX / 2;
+  auto kk_of = [](int k) { return k <= H ? k : NX - k; };
 
   C v[E];
   if (a.mode == ROW_R2C) {
@@ -699,7 +804,12 @@ __device__ __forceinline__ void row_body(const RowArgs<T>& a, int tile, int blk,
     }
   } else if (a.mode == ROW_C2R) {
 #pragma unroll
-    for (int i = 0; i < E; ++i) v[i] = zsrc_c2r<C>(a.A + r0, a.A + r1, reg_pos<NX, RI0, E>(t, i), NX);
+    for (int i = 0; i < E; ++i) {
+      const int k = reg_pos<NX, RI0, E>(t, i);
+      C p, q;
+      ld_pair<PAIRED>(a.A + r0, a.A + r1, kk_of(k) << yl, p, q);
+      v[i] = zpair<false, T>(p, q, k, NX, a.dkx);
+    }
     fft_line<NX, +1, E>(v, t, line, a.tw);
     if (valid) {
 #pragma unroll
@@ -713,62 +823,73 @@ __device__ __forceinline__ void row_body(const RowArgs<T>& a, int tile, int blk,
   } else {  // ROW_RHS / ROW_RHS3
     const bool three = (a.mode == ROW_RHS3);
     if (three) {
-      // c_z of both rows: Z = C0 + i C1 (Hermitian extensions) -> park
+      // c_z of both rows: F^-1 of (C0 + i C1, Hermitian-extended) -> park
 #pragma unroll
-      for (int i = 0; i < E; ++i) v[i] = zsrc_c2r<C>(a.Cin + r0, a.Cin + r1, reg_pos<NX, RI0, E>(t, i), NX);
+      for (int i = 0; i < E; ++i) {
+        const int k = reg_pos<NX, RI0, E>(t, i);
+        C p, q;
+        ld_pair<PAIRED>(a.Cin + r0, a.Cin + r1, kk_of(k) << yl, p, q);
+        v[i] = zpair<false, T>(p, q, k, NX, a.dkx);
+      }
       fft_line<NX, +1, E>(v, t, line, a.tw);
 #pragma unroll
       for (int i = 0; i < E; ++i) park[NX + i * TPL + t] = v[i];
       asm volatile("" ::: "memory");
     }
-    const bool analytic = BATCHED && a.slots[slot].flow_kind == FLOW_CELLULAR;
-    // row y0: c_x + i c_y -> park the product's first half
+    // c_x of both rows (from i kr A) -> park
 #pragma unroll
-    for (int i = 0; i < E; ++i) v[i] = zsrc_rhs<T, C>(a.A + r0, a.B + r0, reg_pos<NX, RI0, E>(t, i), NX, a.dkx);
-    fft_line<NX, +1, E>(v, t, line, a.tw);
-    if (analytic) {
-      const CellularRow<T> cr = cellular_row<T, C>(a.slots[slot], a.tw, yy0, NX, a.stage_c, a.fscale);
-#pragma unroll
-      for (int i = 0; i < E; ++i) {
-        T uu, vv;
-        cellular_uv<T, C>(cr, a.tw, reg_pos<NX, RIL, E>(t, i), NX, &uu, &vv);
-        C pk; pk.x = uu * v[i].x + vv * v[i].y; pk.y = 0;
-        park[i * TPL + t] = pk;
-      }
-    } else {
-#pragma unroll
-      for (int i = 0; i < E; ++i) {
-        const int x = reg_pos<NX, RIL, E>(t, i);
-        T n0 = a.u[foff + q0 + x] * v[i].x + a.v[foff + q0 + x] * v[i].y;
-        if (three) n0 += a.w[foff + q0 + x] * park[NX + i * TPL + t].x;
-        C pk; pk.x = n0; pk.y = 0;
-        park[i * TPL + t] = pk;
-      }
+    for (int i = 0; i < E; ++i) {
+      const int k = reg_pos<NX, RI0, E>(t, i);
+      C p, q;
+      ld_pair<PAIRED>(a.A + r0, a.A + r1, kk_of(k) << yl, p, q);
+      v[i] = zpair<true, T>(p, q, k, NX, a.dkx);
     }
-    asm volatile("" ::: "memory");
-    // row y1
-#pragma unroll
-    for (int i = 0; i < E; ++i) v[i] = zsrc_rhs<T, C>(a.A + r1, a.B + r1, reg_pos<NX, RI0, E>(t, i), NX, a.dkx);
     fft_line<NX, +1, E>(v, t, line, a.tw);
+#pragma unroll
+    for (int i = 0; i < E; ++i) park[i * TPL + t] = v[i];
+    asm volatile("" ::: "memory");
+    // c_y of both rows (from B)
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const int k = reg_pos<NX, RI0, E>(t, i);
+      C p, q;
+      ld_pair<PAIRED>(a.B + r0, a.B + r1, kk_of(k) << yl, p, q);
+      v[i] = zpair<false, T>(p, q, k, NX, a.dkx);
+    }
+    fft_line<NX, +1, E>(v, t, line, a.tw);
+    // keep the flow loads below from being hoisted into the transform (that
+    // holds 4 E more values across it)
+    asm volatile("" ::: "memory");
+    // the products n = -(u.grad c) of rows y0 (Re) and y1 (Im); the flow is
+    // pre-scaled (see the file header)
+    const bool analytic = BATCHED && a.slots[slot].flow_kind == FLOW_CELLULAR;
     if (analytic) {
-      const CellularRow<T> cr = cellular_row<T, C>(a.slots[slot], a.tw, yy0 + 1, NX, a.stage_c, a.fscale);
+      const CellularRow<T> cr0 = cellular_row<T, C>(a.slots[slot], a.tw, yy0, NX, a.stage_c, a.fscale);
+      const CellularRow<T> cr1 = cellular_row<T, C>(a.slots[slot], a.tw, yy0 + 1, NX, a.stage_c, a.fscale);
 #pragma unroll
       for (int i = 0; i < E; ++i) {
-        T uu, vv;
-        cellular_uv<T, C>(cr, a.tw, reg_pos<NX, RIL, E>(t, i), NX, &uu, &vv);
+        T u0, v0, u1, v1;
+        cellular_uv2<T, C>(cr0, cr1, a.tw, reg_pos<NX, RIL, E>(t, i), NX, &u0, &v0, &u1, &v1);
+        const C cx = park[i * TPL + t];
         C w;
-        w.x = park[i * TPL + t].x;
-        w.y = uu * v[i].x + vv * v[i].y;
+        w.x = u0 * cx.x + v0 * v[i].x;
+        w.y = u1 * cx.y + v1 * v[i].y;
         v[i] = w;
       }
     } else {
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const int x = reg_pos<NX, RIL, E>(t, i);
-        T n1 = a.u[foff + q1 + x] * v[i].x + a.v[foff + q1 + x] * v[i].y;
-        if (three) n1 += a.w[foff + q1 + x] * park[NX + i * TPL + t].y;
+        const C cx = park[i * TPL + t];
+        T n0 = a.u[foff + q0 + x] * cx.x + a.v[foff + q0 + x] * v[i].x;
+        T n1 = a.u[foff + q1 + x] * cx.y + a.v[foff + q1 + x] * v[i].y;
+        if (three) {
+          const C cz = park[NX + i * TPL + t];
+          n0 += a.w[foff + q0 + x] * cz.x;
+          n1 += a.w[foff + q1 + x] * cz.y;
+        }
         C w;
-        w.x = park[i * TPL + t].x;
+        w.x = n0;
         w.y = n1;
         v[i] = w;
       }
@@ -789,8 +910,7 @@ __device__ __forceinline__ void row_body(const RowArgs<T>& a, int tile, int blk,
       // row y0: W[k] + conj(W[n-k]) ; row y1: -i (W[k] - conj(W[n-k]))
       o0.x = (wk.x + wn.x) * sc; o0.y = (wk.y - wn.y) * sc;
       o1.x = (wk.y + wn.y) * sc; o1.y = (wn.x - wk.x) * sc;
-      a.out[r0 + k] = o0;
-      a.out[r1 + k] = o1;
+      st_pair<PAIRED>(a.out + r0, a.out + r1, k << yl, o0, o1);
     }
   }
 }
@@ -910,10 +1030,14 @@ __global__ void __launch_bounds__(256) row_rhs_tma_kernel(RowArgs<T> a) {
   }
 }
 
-template <typename T, int NX>
-__global__ void __launch_bounds__(256) row_pass_kernel(RowArgs<T> a) {
+// FP32 row blocks are held to 128 registers (two 256-thread blocks, or eight
+// of the default 64 threads, per SM); FP64 takes what it needs.
+template <typename T> struct RowBounds { static constexpr int blocks = 1; };
+template <> struct RowBounds<float> { static constexpr int blocks = 2; };
+template <typename T, int NX, bool PAIRED = false>
+__global__ void __launch_bounds__(256, RowBounds<T>::blocks) row_pass_kernel(RowArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  row_body<T, NX, false>(a, blockIdx.x, blockIdx.y, smem_raw);
+  row_body<T, NX, false, PAIRED>(a, blockIdx.x, blockIdx.y, smem_raw);
 }
 
 }  // namespace ptf
