@@ -124,9 +124,11 @@ int ptf_set_c(ptf_handle* h, const double* c, int32_t where);
 int ptf_get_c(ptf_handle* h, double* c, int32_t where);
 /* prob.sol out / in (complex, (nx/2+1)*ny[*nz] per solve).  For FP32
  * handles with k0_mode, get_sol reports the FP64 k = 0 mode and set_sol
- * seeds it, so get_sol then set_sol (with ptf_clock / ptf_set_clock) saves
- * and resumes a solve exactly -- the state a FourierFlows snapshot of
- * sol and clock holds. */
+ * seeds it.  An FP32 2D/3D handle holds its state as a compensated pair of
+ * FP32 values; get_sol returns their sum (exact in FP64) and set_sol splits
+ * its input the same way.  So get_sol then set_sol (with ptf_clock /
+ * ptf_set_clock) saves and resumes a solve exactly -- the state a
+ * FourierFlows snapshot of sol and clock holds. */
 int ptf_get_sol(ptf_handle* h, double* sol, int32_t where);
 int ptf_set_sol(ptf_handle* h, const double* sol, int32_t where);
 

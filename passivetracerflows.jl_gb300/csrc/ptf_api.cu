@@ -130,6 +130,7 @@ struct ptf_handle {
   bool own_stream = false;
   // device buffers (compute precision)
   void *s = nullptr, *si = nullptr, *acc = nullptr;
+  void* slo = nullptr;  // FP32 handles: the state's low part (compensated state, stage_combine)
   void *A = nullptr, *B = nullptr, *Nx = nullptr;  // 2D; in 3D A = P1, Nx = P1
   void *C = nullptr;                               // 3D: P2 (Z2 / C)
   void *Ltab = nullptr, *coef = nullptr, *twx = nullptr, *twy = nullptr, *twz = nullptr, *filt = nullptr;
@@ -429,6 +430,8 @@ template <typename T> int run_col(ptf_handle* h, const ColGeom& g, int mode, con
   a.nxin = goff<const C>(io.nxin, h, gr);
   a.s = goff<C>(io.s ? io.s : h->s, h, gr);
   a.si = goff<C>(h->si, h, gr); a.acc = goff<C>(h->acc, h, gr);
+  // the compensated state belongs to the main pass's own state
+  a.slo = (&g == &h->gmain && !io.s) ? goff<C>(h->slo, h, gr) : nullptr;
   a.A = goff<C>(io.A, h, gr); a.B = goff<C>(io.B, h, gr); a.Cout = goff<C>(io.Cout, h, gr);
   a.z2in = goff<const C>(io.z2in, h, gr); a.nout = goff<C>(io.nout, h, gr);
   a.tw = (const C*)(g.axis == 2 ? h->twz : h->twy);
@@ -804,7 +807,7 @@ int check_where(ptf_handle* h, int32_t where) {
   return PTF_OK;
 }
 
-int spec_in(ptf_handle* h, const double* sol, int32_t where, void* dst, const SpecMap& map) {
+int spec_in(ptf_handle* h, const double* sol, int32_t where, void* dst, const SpecMap& map, void* lo = nullptr) {
   const long long rows = h->rows * h->cfg.batch;
   const long long n = rows * h->nkr;
   const double2* src = (const double2*)sol;
@@ -814,7 +817,7 @@ int spec_in(ptf_handle* h, const double* sol, int32_t where, void* dst, const Sp
     if (e != cudaSuccess) return cuda_fail(h, e, "spectral copy");
     src = (const double2*)h->stage;
   }
-  e = h->fp32 ? launch_spec_in<float>(src, (float2*)dst, h->nkr, h->pitch, rows, h->stream, &map, h->rows)
+  e = h->fp32 ? launch_spec_in<float>(src, (float2*)dst, h->nkr, h->pitch, rows, h->stream, &map, h->rows, (float2*)lo)
               : launch_spec_in<double>(src, (double2*)dst, h->nkr, h->pitch, rows, h->stream, &map, h->rows);
   h->launches++;
   if (e != cudaSuccess) return cuda_fail(h, e, "spectral convert");
@@ -822,11 +825,13 @@ int spec_in(ptf_handle* h, const double* sol, int32_t where, void* dst, const Sp
 }
 
 // k0patch: the (0,0[,0]) element of each solve comes from the FP64 k = 0 state
-int spec_out(ptf_handle* h, const void* src, double* user, int32_t where, const SpecMap& map, bool k0patch = false) {
+int spec_out(ptf_handle* h, const void* src, double* user, int32_t where, const SpecMap& map, bool k0patch = false,
+             const void* lo = nullptr) {
   const long long rows = h->rows * h->cfg.batch;
   const long long n = rows * h->nkr;
   double2* dst = (where == PTF_HOST) ? (double2*)h->stage : (double2*)user;
-  cudaError_t e = h->fp32 ? launch_spec_out<float>((const float2*)src, dst, h->nkr, h->pitch, rows, h->stream, &map, h->rows)
+  cudaError_t e = h->fp32 ? launch_spec_out<float>((const float2*)src, dst, h->nkr, h->pitch, rows, h->stream, &map, h->rows,
+                                                   (const float2*)lo)
                           : launch_spec_out<double>((const double2*)src, dst, h->nkr, h->pitch, rows, h->stream, &map, h->rows);
   h->launches++;
   if (e == cudaSuccess && k0patch) {
@@ -930,9 +935,13 @@ template <typename T> int time_steps(ptf_handle* h, int steps, double* ms) {
 template <typename T> int autotune_impl(ptf_handle* h, int steps) {
   typedef typename cplx_of<T>::type C;
   const size_t sbytes = (size_t)h->plane * h->bpad * sizeof(C);
+  const size_t nparts = h->slo ? 2 : 1;  // the state and, when compensated, its low part
   void* saved = nullptr;
   double* saved_k0 = nullptr;
-  if (cudaMalloc(&saved, sbytes) != cudaSuccess) { cudaGetLastError(); return fail(h, PTF_ERR_MEMORY, "tuning: state copy"); }
+  if (cudaMalloc(&saved, nparts * sbytes) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(h, PTF_ERR_MEMORY, "tuning: state copy");
+  }
   if (h->k0mode && cudaMalloc((void**)&saved_k0, 4 * sizeof(double) * h->bpad) != cudaSuccess) {
     cudaGetLastError();
     cudaFree(saved);
@@ -941,6 +950,8 @@ template <typename T> int autotune_impl(ptf_handle* h, int steps) {
   const double t0 = h->t;
   const long long step0 = h->step;
   cudaError_t e = cudaMemcpyAsync(saved, h->s, sbytes, cudaMemcpyDeviceToDevice, h->stream);
+  if (e == cudaSuccess && h->slo)
+    e = cudaMemcpyAsync((char*)saved + sbytes, h->slo, sbytes, cudaMemcpyDeviceToDevice, h->stream);
   if (e == cudaSuccess && saved_k0)
     e = cudaMemcpyAsync(saved_k0, h->k0, 4 * sizeof(double) * h->bpad, cudaMemcpyDeviceToDevice, h->stream);
   int rc = e == cudaSuccess ? PTF_OK : cuda_fail(h, e, "tuning: save state");
@@ -976,6 +987,8 @@ template <typename T> int autotune_impl(ptf_handle* h, int steps) {
   if (!rc) rc = apply_tuning(h, best);
   // restore the solve
   e = cudaMemcpyAsync(h->s, saved, sbytes, cudaMemcpyDeviceToDevice, h->stream);
+  if (e == cudaSuccess && h->slo)
+    e = cudaMemcpyAsync(h->slo, (char*)saved + sbytes, sbytes, cudaMemcpyDeviceToDevice, h->stream);
   if (e == cudaSuccess && saved_k0)
     e = cudaMemcpyAsync(h->k0, saved_k0, 4 * sizeof(double) * h->bpad, cudaMemcpyDeviceToDevice, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -1108,6 +1121,7 @@ int ptf_create(const ptf_config* cfg, ptf_handle** out) {
   const size_t sp = (size_t)h->nphys * B * elem_r(h);
   bool ok = true;
   ok = ok && dev_alloc(h, &h->s, sc) && dev_alloc(h, &h->si, sc) && dev_alloc(h, &h->acc, sc);
+  if (h->fp32 && h->dim >= 2) ok = ok && dev_alloc(h, &h->slo, sc);
   ok = ok && dev_alloc(h, &h->A, sc);
   if (h->dim >= 2) ok = ok && dev_alloc(h, &h->B, sc);
   if (h->dim == 2) ok = ok && dev_alloc(h, &h->Nx, sc);
@@ -1258,14 +1272,14 @@ int ptf_get_sol(ptf_handle* h, double* sol, int32_t where) {
   if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
   if (!sol) return fail(h, PTF_ERR_ARG, "null field");
   if (check_where(h, where)) return PTF_ERR_ARG;
-  return spec_out(h, h->s, sol, where, state_map(h), h->k0mode);
+  return spec_out(h, h->s, sol, where, state_map(h), h->k0mode, h->slo);  // s + its low part, exact in FP64
 }
 
 int ptf_set_sol(ptf_handle* h, const double* sol, int32_t where) {
   if (!h) return fail(nullptr, PTF_ERR_ARG, "null handle");
   if (!sol) return fail(h, PTF_ERR_ARG, "null field");
   if (check_where(h, where)) return PTF_ERR_ARG;
-  int rc = spec_in(h, sol, where, h->s, state_map(h));
+  int rc = spec_in(h, sol, where, h->s, state_map(h), h->slo);  // split into s and its low part
   if (rc) return rc;
   if (h->k0mode) {
     const double2* src = where == PTF_HOST ? (const double2*)h->stage : (const double2*)sol;

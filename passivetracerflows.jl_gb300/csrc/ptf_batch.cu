@@ -45,6 +45,11 @@ template <typename T> __global__ void batch_clock_kernel(SlotParams<T>* slots, i
   s.t += s.dtd;
   s.step += 1;
   if (s.step >= s.nsteps) s.active = 0;
+  else if (s.flow_kind == FLOW_CELLULAR) slot_phases(s);
+}
+// The flow phases of one slot after its parameters were uploaded.
+template <typename T> __global__ void batch_phase_kernel(SlotParams<T>* slot) {
+  if (slot->flow_kind == FLOW_CELLULAR) slot_phases(*slot);
 }
 
 #define PTF_EXTERN_STAGE(T, M)                                                                              \
@@ -74,6 +79,7 @@ struct Bucket {
   double L = 0;
   void *s = nullptr, *si = nullptr, *acc = nullptr, *A = nullptr, *B = nullptr, *Nx = nullptr;
   void *u = nullptr, *v = nullptr, *phys = nullptr, *tw = nullptr;
+  void* slo = nullptr;             // FP32: the state's low part (compensated state, stage_combine)
   int slot_base = 0;               // first entry of the bucket in the slot parameter array
   std::vector<long long> owner;    // solve id per slot, -1 when free
   int W = 1, P = 1;                // single-slot launch shapes (admission, readback)
@@ -164,7 +170,7 @@ void free_bucket(ptf_batch* b, Bucket& k) {
   k.allocs.clear();
   b->bytes -= std::min(b->bytes, k.alloc_bytes);
   k.alloc_bytes = 0;
-  k.s = k.si = k.acc = k.A = k.B = k.Nx = k.u = k.v = k.phys = k.tw = nullptr;
+  k.s = k.si = k.acc = k.A = k.B = k.Nx = k.u = k.v = k.phys = k.tw = k.slo = nullptr;
   k.dead = true;
   k.n = 0;
   b->bucket_gen++;
@@ -184,7 +190,7 @@ void reclaim_empty_buckets(ptf_batch* b) {
 
 size_t per_slot_bytes(const ptf_batch* b, int n) {
   const int pitch = ((n / 2 + 1) + 7) / 8 * 8;
-  return 6 * (size_t)n * pitch * ec(b) + 3 * (size_t)n * n * er(b);
+  return (b->fp32 ? 7 : 6) * (size_t)n * pitch * ec(b) + 3 * (size_t)n * n * er(b);
 }
 
 void host_twiddles_d(std::vector<double>& out, int n) {
@@ -244,7 +250,7 @@ int new_bucket(ptf_batch* b, int n, double L) {
   bool ok = bucket_alloc(b, k, &k.s, sc) && bucket_alloc(b, k, &k.si, sc) && bucket_alloc(b, k, &k.acc, sc) &&
             bucket_alloc(b, k, &k.A, sc) && bucket_alloc(b, k, &k.B, sc) && bucket_alloc(b, k, &k.Nx, sc) &&
             bucket_alloc(b, k, &k.u, sp) && bucket_alloc(b, k, &k.v, sp) && bucket_alloc(b, k, &k.phys, sp) &&
-            bucket_alloc(b, k, &k.tw, (size_t)n * ec(b));
+            bucket_alloc(b, k, &k.tw, (size_t)n * ec(b)) && (!b->fp32 || bucket_alloc(b, k, &k.slo, sc));
   if (!ok) {
     cudaStreamSynchronize(b->stream);
     for (void* p : k.allocs) cudaFree(p);
@@ -299,6 +305,14 @@ template <typename T> int upload_slot(ptf_batch* b, int g) {
   if (e != cudaSuccess) return bcuda(b, e, "slot upload");
   return PTF_OK;
 }
+// One slot's device parameters back into the host copy.
+template <typename T> int download_slot(ptf_batch* b, int g) {
+  cudaError_t e = cudaMemcpyAsync(&host_slot<T>(b, g), (SlotParams<T>*)b->slots_dev + g, sizeof(SlotParams<T>),
+                                  cudaMemcpyDeviceToHost, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return bcuda(b, e, "slot download");
+  return PTF_OK;
+}
 template <typename T> int download_slots(ptf_batch* b) {
   cudaError_t e = cudaMemcpyAsync(b->slots_host.data(), b->slots_dev, (size_t)b->slot_used * sizeof(SlotParams<T>),
                                   cudaMemcpyDeviceToHost, b->stream);
@@ -314,9 +328,11 @@ template <typename T> ColArgs<T> slot_col(ptf_batch* b, const Bucket& k, int slo
   std::memset(&a, 0, sizeof(a));
   const size_t off = (size_t)slot * k.n * k.pitch;
   a.s = (C*)k.s + off; a.si = (C*)k.si + off; a.acc = (C*)k.acc + off;
+  a.slo = k.slo ? (C*)k.slo + off : nullptr;
   a.A = (C*)k.A + off; a.B = (C*)k.B + off; a.nxin = (C*)k.Nx + off;
   a.tw = (const C*)k.tw;
   a.stride = k.pitch; a.mode = mode; a.do_inverse = 1;
+  a.ylog = kBatchYlog; a.priv = 1;  // the single-handle layouts (spec_index, SpecMap)
   a.bstride = (long long)k.n * k.pitch; a.tplane = a.bstride;
   (void)b;
   return a;
@@ -329,7 +345,7 @@ template <typename T> RowArgs<T> slot_row(ptf_batch* b, const Bucket& k, int slo
   a.A = (const C*)k.A + off; a.out = (C*)k.Nx + off;
   a.cin = (const T*)k.phys + poff; a.cout = (T*)k.phys + poff;
   a.tw = (const C*)k.tw;
-  a.rows = k.n; a.pitch = k.pitch; a.mode = mode; a.park_slots = 1;
+  a.rows = k.n; a.pitch = k.pitch; a.mode = mode; a.park_slots = 1; a.ylog = kBatchYlog;
   a.bstride = (long long)k.n * k.pitch; a.pstride = (long long)k.n * k.n;
   (void)b;
   return a;
@@ -390,7 +406,14 @@ template <typename T> int admit(ptf_batch* b, Bucket& k, int slot, const ptf_sol
   sp.active = d.nsteps > 0 ? 1 : 0;
   k.owner[slot] = id;
   b->plan_dirty = true;
-  return upload_slot<T>(b, g);
+  int rc = upload_slot<T>(b, g);
+  if (rc) return rc;
+  batch_phase_kernel<T><<<1, 1, 0, b->stream>>>((SlotParams<T>*)b->slots_dev + g);
+  b->launches++;
+  e = cudaStreamSynchronize(b->stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return bcuda(b, e, "slot phases");
+  return download_slot<T>(b, g);
 }
 
 // Rebuild the work plan over the slots that are still active.
@@ -419,8 +442,10 @@ template <typename T> int build_plan(ptf_batch* b) {
     (void)tplN;
     ColArgs<T>& c = bp.col;
     c.s = (C*)k.s; c.si = (C*)k.si; c.acc = (C*)k.acc; c.A = (C*)k.A; c.B = (C*)k.B; c.nxin = (const C*)k.Nx;
+    c.slo = (C*)k.slo;
     c.tw = (const C*)k.tw;
     c.stride = k.pitch; c.do_inverse = 1;
+    c.ylog = kBatchYlog; c.priv = 1;
     c.bstride = (long long)k.n * k.pitch; c.tplane = c.bstride;
     c.slots = (const SlotParams<T>*)b->slots_dev + k.slot_base;
     c.k0 = b->k0mode ? b->k0 + 4 * (size_t)k.slot_base : nullptr;
@@ -432,7 +457,7 @@ template <typename T> int build_plan(ptf_batch* b) {
     r.tw = (const C*)k.tw;
     r.dkx = (T)0;  // set below from the bucket's first solve (square, same L per bucket)
     r.scale = (T)1;
-    r.rows = k.n; r.pitch = k.pitch; r.mode = ROW_RHS; r.park_slots = 1;
+    r.rows = k.n; r.pitch = k.pitch; r.mode = ROW_RHS; r.park_slots = 1; r.ylog = kBatchYlog;
     r.bstride = c.bstride; r.pstride = (long long)k.n * k.n; r.fstride = r.pstride;
     r.slots = c.slots;
     r.nslots = c.nslots;

@@ -10,6 +10,10 @@ namespace ptf {
 
 constexpr int kBatchThreads = 256;
 constexpr int kMaxBuckets = 32;
+// Slot fields use the single-handle layouts: rows interleaved in fours
+// (every bucket size is >= 64) and the state in the column pass's register
+// order.
+constexpr int kBatchYlog = 2;
 
 template <typename T> struct BucketPlan {
   ColArgs<T> col;
@@ -56,7 +60,7 @@ template <typename T, int N>
 __device__ __noinline__ void batch_row_item(const RowArgs<T>* ra, T stage_c, int local, unsigned char* smem) {
   RowArgs<T> a = *ra;
   a.stage_c = stage_c;
-  row_body<T, N, true>(a, local, 0, smem);
+  row_body<T, N, true, true>(a, local, 0, smem);
 }
 template <typename T, int N, int MODE>
 __device__ __noinline__ void batch_col_item(const ColArgs<T>* ca, int local, unsigned char* smem) {
@@ -135,7 +139,7 @@ batch_row_kernel(const BatchPlan<T>* __restrict__ plan, T stage_c) {
   ra.stage_c = stage_c;
   const int local = item - plan->b[b].row_begin;
   switch (plan->b[b].n) {
-#define PTF_CASE(n) case n: row_body<T, n, true>(ra, local, 0, smem); break;
+#define PTF_CASE(n) case n: row_body<T, n, true, true>(ra, local, 0, smem); break;
     PTF_BATCH_SIZES(PTF_CASE)
 #undef PTF_CASE
     default: break;
@@ -148,11 +152,12 @@ batch_col_kernel(const BatchPlan<T>* __restrict__ plan) {
   const int item = plan->row_total + blockIdx.x, nb = plan->nb;
   int b = 0;
   while (b + 1 < nb && item >= plan->b[b + 1].col_begin) ++b;
-  const ColArgs<T> ca = plan->b[b].col;
   const int local = item - plan->b[b].col_begin;
+  // each size's body as a real call (batch_col_item): inlined side by side
+  // in one kernel they shared one register allocation and spilled 370-540 B
+  // per thread in the RK4 stages 2-4; as calls, 0-28 B
   switch (plan->b[b].n) {
-    // buckets hold square grids: the row pitch is square_pitch<n>()
-#define PTF_CASE(n) case n: col_body<T, n, MODE, true, square_pitch<n>()>(ca, local, 0, smem); break;
+#define PTF_CASE(n) case n: batch_col_item<T, n, MODE>(&plan->b[b].col, local, smem); break;
     PTF_BATCH_SIZES(PTF_CASE)
 #undef PTF_CASE
     default: break;

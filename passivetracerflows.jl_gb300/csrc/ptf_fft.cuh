@@ -52,9 +52,10 @@ template <typename C> __device__ __forceinline__ C cmul_plain(C a, C b) {
   r.y = a.x * b.y + a.y * b.x;
   return r;
 }
-// FP32 stages of radix >= 8 load the power-of-two powers of a butterfly's
-// twiddle and multiply out the rest (1): fewer table loads and far fewer
-// live registers.
+// FP32 stages of radix 8 and 16 apply a butterfly's twiddles W^r in a
+// factored form (twiddled_dft below): only table values, none formed by
+// multiplying rounded twiddles together.  PTF_TW_POW2 (radix 32 only, FP32)
+// loads the power-of-two powers and multiplies out the rest.
 #ifndef PTF_TW_POW2
 #define PTF_TW_POW2 1
 #endif
@@ -192,6 +193,75 @@ template <int DIR, typename C> struct DFT<32, DIR, C> {
   }
 };
 
+// A radix-16 or radix-8 Stockham butterfly with its input twiddles
+// t_r = W^r (W = this butterfly's base twiddle, r = 0..R-1) applied in
+// factored form.  The DFT splits r = n2 + 4 n1 (inner DFT over n1, the
+// stride-4 elements; outer over n2): t_r = W^(4 n1) W^n2, and W^n2 is
+// constant across each inner DFT, so it is applied to the inner DFT's
+// outputs instead of its inputs.  The twiddles used are W, W^2, W^3, W^4,
+// W^8, W^12 (radix 16) or W..W^4 (radix 8), each a correctly rounded table
+// value: no twiddle is a product of rounded twiddles.  Radix 16: 24 complex
+// products (the direct form needs 15, plus 11 to build W^r from four table
+// values), 6 table loads.  Same arithmetic as DFT<R> after the twiddles.
+template <int R, int DIR, typename C> struct TwiddledDFT;
+template <int DIR, typename C> struct TwiddledDFT<16, DIR, C> {
+  static __device__ __forceinline__ void run(C* v, const C* __restrict__ tw, int b) {
+    const C w1 = __ldg(tw + b), w2 = __ldg(tw + 2 * b), w3 = __ldg(tw + 3 * b);
+    const C w4 = __ldg(tw + 4 * b), w8 = __ldg(tw + 8 * b), w12 = __ldg(tw + 12 * b);
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) {
+      v[n2 + 4] = cmul_tw<DIR>(v[n2 + 4], w4);
+      v[n2 + 8] = cmul_tw<DIR>(v[n2 + 8], w8);
+      v[n2 + 12] = cmul_tw<DIR>(v[n2 + 12], w12);
+      dft4<DIR>(v[n2], v[n2 + 4], v[n2 + 8], v[n2 + 12]);
+    }
+    // y[n2][k1] in v[n2 + 4*k1]: times W^n2, then the internal twiddle w16^(n2*k1)
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+      v[1 + 4 * k1] = cmul_tw<DIR>(v[1 + 4 * k1], w1);
+      v[2 + 4 * k1] = cmul_tw<DIR>(v[2 + 4 * k1], w2);
+      v[3 + 4 * k1] = cmul_tw<DIR>(v[3 + 4 * k1], w3);
+    }
+    v[5] = rot16<DIR, 1>(v[5]);  v[6] = rot16<DIR, 2>(v[6]);  v[7] = rot16<DIR, 3>(v[7]);
+    v[9] = rot16<DIR, 2>(v[9]);  v[10] = rot16<DIR, 4>(v[10]); v[11] = rot16<DIR, 6>(v[11]);
+    v[13] = rot16<DIR, 3>(v[13]); v[14] = rot16<DIR, 6>(v[14]); v[15] = rot16<DIR, 9>(v[15]);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) dft4<DIR>(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+    C t[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) t[i] = v[i];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+      for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = t[4 * k1 + k2];
+  }
+};
+template <int DIR, typename C> struct TwiddledDFT<8, DIR, C> {
+  static __device__ __forceinline__ void run(C* v, const C* __restrict__ tw, int b) {
+    const C w1 = __ldg(tw + b), w2 = __ldg(tw + 2 * b), w3 = __ldg(tw + 3 * b), w4 = __ldg(tw + 4 * b);
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) {
+      v[n2 + 4] = cmul_tw<DIR>(v[n2 + 4], w4);
+      dft2<DIR>(v[n2], v[n2 + 4]);
+    }
+    // y[n2][k1] in v[n2 + 4*k1]: times W^n2, then the internal twiddle w8^(n2*k1)
+#pragma unroll
+    for (int k1 = 0; k1 < 2; ++k1) {
+      v[1 + 4 * k1] = cmul_tw<DIR>(v[1 + 4 * k1], w1);
+      v[2 + 4 * k1] = cmul_tw<DIR>(v[2 + 4 * k1], w2);
+      v[3 + 4 * k1] = cmul_tw<DIR>(v[3 + 4 * k1], w3);
+    }
+    v[5] = rot16<DIR, 2>(v[5]); v[6] = rot16<DIR, 4>(v[6]); v[7] = rot16<DIR, 6>(v[7]);
+    dft4<DIR>(v[0], v[1], v[2], v[3]);
+    dft4<DIR>(v[4], v[5], v[6], v[7]);
+    C t[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) t[i] = v[i];
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) { v[2 * k2] = t[k2]; v[2 * k2 + 1] = t[4 + k2]; }
+  }
+};
+
 constexpr int FFT_E = 16;  // default complex values per thread
 
 // Values per thread of the row (and 1D, batched) passes: 16; FP32 lengths
@@ -235,6 +305,11 @@ __device__ __forceinline__ void stage_compute(C* v, int t, const C* __restrict__
 #pragma unroll
   for (int q = 0; q < E / R; ++q) {
     const int j = t + q * (N / E);
+    if constexpr (NS > 1 && (R == 8 || R == 16) && sizeof(C) == 8) {
+      // FP32: twiddles applied in factored form inside the butterfly
+      TwiddledDFT<R, DIR, C>::run(v + q * R, tw, (j % NS) * (N / (NS * R)));
+      continue;
+    }
     if (NS > 1) {
       const int k = j % NS;
       if (PTF_TW_POW2 && R >= 8 && sizeof(v[0].x) == 4) {

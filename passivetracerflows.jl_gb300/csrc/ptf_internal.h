@@ -47,12 +47,16 @@ template <typename T> cudaError_t launch_real_out(const T* src, double* dst, lon
 // user spectral layout (nkr complex per row) <-> pitched internal layout:
 // the plain [rows][pitch] layout without a map, else spec_map(*map, r, k)
 // within each solve of rows_per_solve rows
+// (lo: the low part of a compensated state, written as the FP64 value's
+// remainder after rounding / added back; null: none)
 template <typename T>
 cudaError_t launch_spec_in(const double2* src, typename cplx_of<T>::type* dst, int nkr, int pitch, long long rows,
-                           cudaStream_t st, const SpecMap* map = nullptr, long long rows_per_solve = 0);
+                           cudaStream_t st, const SpecMap* map = nullptr, long long rows_per_solve = 0,
+                           typename cplx_of<T>::type* lo = nullptr);
 template <typename T>
 cudaError_t launch_spec_out(const typename cplx_of<T>::type* src, double2* dst, int nkr, int pitch, long long rows,
-                            cudaStream_t st, const SpecMap* map = nullptr, long long rows_per_solve = 0);
+                            cudaStream_t st, const SpecMap* map = nullptr, long long rows_per_solve = 0,
+                            const typename cplx_of<T>::type* lo = nullptr);
 
 // FP64 k = 0 mode (ptf_util.cu).  Per-solve sums of x (n values per solve):
 // out[b * out_stride]; partials holds 64 doubles per solve.

@@ -23,7 +23,7 @@ template <typename T, int N> struct PassLaunch {
   static cudaError_t col_k(const ColArgs<T>& a, int W, int nbx, int batch, cudaStream_t st, int carve) {
     auto kern = col_pass_kernel<T, N, MODE, CS>;
     if (W * col_tpl<T, N>() > max_threads(kern)) return cudaErrorInvalidConfiguration;
-    const size_t smem = col_smem_bytes<T, N>(W);
+    const size_t smem = col_smem_bytes_mode<T, N>(W, MODE);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, carve < 0 ? -1 : carve);
     if (e != cudaSuccess) return e;
@@ -89,7 +89,7 @@ template <typename T, int N> struct PassLaunch {
 
 template <typename T, int N> int max_lines_n(bool col) {
   typedef typename cplx_of<T>::type C;
-  const size_t lb = col ? col_smem_bytes<T, N>(1) : row_smem_bytes<T, N>(1, 2);
+  const size_t lb = col ? col_smem_bytes_mode<T, N>(1, COL_ETD_4) : row_smem_bytes<T, N>(1, 2);
   (void)sizeof(C);
   int m = (int)((200u * 1024u) / lb);
   const int tpl = col ? col_tpl<T, N>() : pass_tpl<T, N>();

@@ -90,6 +90,37 @@ __global__ void __launch_bounds__(256) line1d_kernel(Line1DArgs<T> a) {
     v[i].x *= uu;
     v[i].y *= uu;
   }
+  // FP64 k = 0 mode: N(0) of both solves as compensated FP64 sums of the
+  // products (Re: solve y0, Im: solve y1) rather than the FP32 transform's
+  // k = 0 bin; they land in the pair's thread t = 0, which handles k = 0.
+  double n0sum[2] = {0.0, 0.0};
+  if (a.k0 != nullptr && MODE != COL_FWD_N) {  // uniform across the block
+    double* part = reinterpret_cast<double*>(line);  // 2 TPL doubles fit in the line
+    double s0 = 0, c0 = 0, s1 = 0, c1 = 0;
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      double y = (double)v[i].x - c0, u0 = s0 + y;
+      c0 = (u0 - s0) - y; s0 = u0;
+      y = (double)v[i].y - c1; const double u1 = s1 + y;
+      c1 = (u1 - s1) - y; s1 = u1;
+    }
+    part[2 * t] = s0;
+    part[2 * t + 1] = s1;
+    __syncthreads();
+    if (t == 0) {
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        double tot = 0, c = 0;
+        for (int q = 0; q < TPL; ++q) {
+          const double y = part[2 * q + j] - c, u = tot + y;
+          c = (u - tot) - y;
+          tot = u;
+        }
+        n0sum[j] = 2.0 * tot;  // the k = 0 bin of the separated spectra is twice the sum
+      }
+    }
+    __syncthreads();
+  }
   fft_line<NX, -1, E>(v, t, line, a.tw);
   __syncthreads();
 #pragma unroll
@@ -115,7 +146,7 @@ __global__ void __launch_bounds__(256) line1d_kernel(Line1DArgs<T> a) {
                                  [&]() { return a.Ltab[k]; }, a.filt);
       if (a.k0 != nullptr && k == 0) {
         double* q = a.k0 + (size_t)(y0 + j) * 4;
-        const double xd = k0_combine<MODE>(q, a.k0c, a.dt64, (double)o[j].x);
+        const double xd = k0_combine<MODE>(q, a.k0c, a.dt64, n0sum[j]);
         x.x = (T)xd; x.y = 0;
         if (MODE == COL_RK4_4 || MODE == COL_ETD_4) a.s[r] = x;
         else if (MODE == COL_RK4_1 || MODE == COL_RK4_2 || MODE == COL_RK4_3) a.si[r] = x;

@@ -95,7 +95,22 @@ template <typename T> struct SlotParams {
   T U, eps, omega;          // FLOW_CELLULAR: psi = U cos(Kx x + eps sin(omega t)) cos(Ky y)
   int nkappah, active, flow_kind, time_mode;
   int Kx, Ky;
+  // FLOW_CELLULAR: cos and sin of the phase eps sin(omega te) at the stage
+  // times te = t + c dt, c = 0, 1/2, 1 (all at t in clock.t mode); set by
+  // slot_phases whenever t changes, so the passes evaluate no trigonometry
+  T ph_c[3], ph_s[3];
 };
+
+__device__ __forceinline__ void sin_cos(double x, double* s, double* c) { sincos(x, s, c); }
+__device__ __forceinline__ void sin_cos(float x, float* s, float* c) { sincosf(x, s, c); }
+template <typename T> __device__ __forceinline__ void slot_phases(SlotParams<T>& sp) {
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const double te = sp.t + (sp.time_mode ? 0.5 * q * (double)sp.dt : 0.0);
+    const T phi = sp.eps * (T)sin((double)sp.omega * te);
+    sin_cos(phi, &sp.ph_s[q], &sp.ph_c[q]);
+  }
+}
 
 template <typename T> struct ColArgs {
   typedef typename cplx_of<T>::type C;
@@ -103,6 +118,7 @@ template <typename T> struct ColArgs {
   C* s;            // state (sol); COL_YINV3: the z-inverse Z1
   C* si;           // RK4: current stage input; ETDRK4: d = E2 a - zeta N(sol)
   C* acc;          // accumulator of the update
+  C* slo;          // FP32 compensated state: the low part of s (null: s alone; see stage_combine)
   const T* filt;   // filtered steppers: the spectral filter the new state is multiplied by (null: none)
   C* A;            // F^-1(s_next)
   C* B;            // F^-1(i k s_next)
@@ -199,6 +215,12 @@ template <> struct ColBounds<float> { static constexpr int threads = PTF_COL_THR
 // between the two inverse transforms.
 template <typename T, int N> __host__ __device__ constexpr size_t col_smem_bytes(int W) {
   return (size_t)W * (line_stride(N) + N) * sizeof(typename cplx_of<T>::type);
+}
+// The stepper's last stage parks one more operand (the state, for the
+// compensated sum): its blocks take a second slot array.
+__host__ __device__ constexpr bool col_second_park(int mode) { return mode == COL_RK4_4 || mode == COL_ETD_4; }
+template <typename T, int N> __host__ __device__ constexpr size_t col_smem_bytes_mode(int W, int mode) {
+  return col_smem_bytes<T, N>(W) + (col_second_park(mode) ? (size_t)W * N * sizeof(typename cplx_of<T>::type) : 0);
 }
 // Values per thread of the column pass (may differ from the row pass's: the
 // column pass is bound by latency, the row pass by shared-memory traffic).
@@ -304,21 +326,63 @@ __host__ __device__ constexpr int early_operand(int mode) {
          : (mode == COL_ETD_4) ? 3 : 0;
 }
 
-template <typename T, int MODE, int PF = 0, typename C, typename LF>
+// hi + lo += d for a state held as a pair with hi = RN(hi + lo): Knuth's
+// two-sum of hi and d, its error added to lo, then renormalised (Dekker's
+// fast two-sum), so the pair stays canonical and round-trips through FP64.
+template <typename T> __device__ __forceinline__ void add_compensated(T& hi, T& lo, T d) {
+  const T t = hi + d;
+  const T bp = t - hi;
+  const T err = (hi - (t - bp)) + (d - bp);
+  const T l = lo + err;
+  hi = t + l;
+  lo = l - (hi - t);
+}
+
+// SLO non-null (FP32 handles): the state is the pair s + s_lo, AC holds only
+// the step's increment (not s plus it), and the last stage adds the
+// increment to the pair with add_compensated.  Rounding the state to FP32
+// then no longer costs half an ulp of s every step: over the 1000 ETDRK4
+// steps of the 1024^2 cellular workload that rounding, fed back through the
+// FP32 transforms, was most of the FP32 error against the FP64 oracle
+// (NumPy emulation: 1.1e-5 with an FP32 state, 2.0e-6 with an FP64 one).
+template <typename T, int MODE, int PF = 0, bool PS = false, typename C, typename LF>
 __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S, C* __restrict__ SI,
                                            C* __restrict__ AC, const T* __restrict__ cf,
                                            size_t plane, T dt, bool store, LF&& Lf,
-                                           const T* __restrict__ filt = nullptr, C pre = C()) {
+                                           const T* __restrict__ filt = nullptr, C pre = C(),
+                                           C* __restrict__ SLO = nullptr, C pre_s = C()) {
+  // PS: the state at o was fetched ahead too (compensated last stage): pre_s
   // PF != 0: operand early_operand(MODE) was fetched ahead; its value is `pre`
   auto ldS = [&]() { return PF == 1 ? pre : S[o]; };
   auto ldSI = [&]() { return PF == 2 ? pre : SI[o]; };
   auto ldAC = [&]() { return PF == 3 ? pre : AC[o]; };
+  const bool comp = SLO != nullptr;
+  // the new state from d (last stage): s + d as a compensated pair, or d
+  // itself (AC carried s), then the filter
+  auto finish = [&](C d) -> C {
+    C hi;
+    if (comp) {
+      hi = PS ? pre_s : S[o];
+      C lo = SLO[o];
+      add_compensated(hi.x, lo.x, d.x);
+      add_compensated(hi.y, lo.y, d.y);
+      if (filt) { const T f = filt[o]; hi.x *= f; hi.y *= f; lo.x *= f; lo.y *= f; }
+      if (store) SLO[o] = lo;
+    } else {
+      hi = d;
+      if (filt) { const T f = filt[o]; hi.x *= f; hi.y *= f; }
+    }
+    if (store) S[o] = hi;
+    return hi;
+  };
   C x;
   if (MODE == COL_RK4_1) {
     const T L = Lf();
     const C s = ldS();
     C k; k.x = L * s.x + Nh.x; k.y = L * s.y + Nh.y;
-    C ac; ac.x = s.x + (dt / 6) * k.x; ac.y = s.y + (dt / 6) * k.y;
+    C ac;
+    if (comp) { ac.x = (dt / 6) * k.x; ac.y = (dt / 6) * k.y; }
+    else { ac.x = s.x + (dt / 6) * k.x; ac.y = s.y + (dt / 6) * k.y; }
     x.x = s.x + (dt / 2) * k.x; x.y = s.y + (dt / 2) * k.y;
     if (store) { AC[o] = ac; SI[o] = x; }
   } else if (MODE == COL_RK4_2 || MODE == COL_RK4_3) {
@@ -334,16 +398,17 @@ __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S,
     const T L = Lf();
     const C si = ldSI(), ac = ldAC();
     C k; k.x = L * si.x + Nh.x; k.y = L * si.y + Nh.y;
-    x.x = ac.x + (dt / 6) * k.x; x.y = ac.y + (dt / 6) * k.y;
-    if (filt) { const T f = filt[o]; x.x *= f; x.y *= f; }
-    if (store) S[o] = x;
+    C d; d.x = ac.x + (dt / 6) * k.x; d.y = ac.y + (dt / 6) * k.y;
+    x = finish(d);
   } else if (MODE == COL_ETD_1) {
     // a = E2 s + zeta N(s) is the next input; stage 3's
     // c = E2 a + zeta (2 N(b) - N(s)) = d + 2 zeta N(b) needs only
     // d = E2 a - zeta N(s), stored in SI in place of a and N(s)
     const T Em = cf[o], E2m = cf[o + plane], ze = cf[o + 2 * plane], al = cf[o + 3 * plane];
     const C s = ldS();
-    C ac; ac.x = (s.x + Em * s.x) + al * Nh.x; ac.y = (s.y + Em * s.y) + al * Nh.y;
+    C ac;
+    if (comp) { ac.x = Em * s.x + al * Nh.x; ac.y = Em * s.y + al * Nh.y; }
+    else { ac.x = (s.x + Em * s.x) + al * Nh.x; ac.y = (s.y + Em * s.y) + al * Nh.y; }
     AC[o] = ac;
     x.x = (s.x + E2m * s.x) + ze * Nh.x; x.y = (s.y + E2m * s.y) + ze * Nh.y;
     C d; d.x = (x.x + E2m * x.x) - ze * Nh.x; d.y = (x.y + E2m * x.y) - ze * Nh.y;
@@ -365,9 +430,8 @@ __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S,
   } else {  // COL_ETD_4
     const T ga = cf[o + 5 * plane];
     const C ac = ldAC();
-    x.x = ac.x + ga * Nh.x; x.y = ac.y + ga * Nh.y;
-    if (filt) { const T f = filt[o]; x.x *= f; x.y *= f; }
-    S[o] = x;
+    C d; d.x = ac.x + ga * Nh.x; d.y = ac.y + ga * Nh.y;
+    x = finish(d);
   }
   return x;
 }
@@ -472,10 +536,20 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
 #define PTF_EARLY_OPERAND_BATCHED 1
 #endif
   constexpr int PF = (PTF_EARLY_OPERAND && (!BATCHED || PTF_EARLY_OPERAND_BATCHED)) ? early_operand(MODE) : 0;
+  // the compensated last stage also reads the state: fetched into a second
+  // slot array (single-solve form; col_smem_bytes_mode sizes it)
+  constexpr bool PS2 = PF != 0 && !BATCHED && col_second_park(MODE);
+  C* park2 = park + W * N;
+  const bool ps = PS2 && a.slo != nullptr;  // uniform across the block
   if (PF) {
     const C* __restrict__ op = (PF == 1 ? a.s : PF == 2 ? a.si : a.acc) + boff;
 #pragma unroll
     for (int i = 0; i < E; ++i) cp_async<sizeof(C)>(park + i * nthr + threadIdx.x, op + PTF_POFF(i));
+    if (PS2 && ps) {
+      const C* __restrict__ sp = a.s + boff;
+#pragma unroll
+      for (int i = 0; i < E; ++i) cp_async<sizeof(C)>(park2 + i * nthr + threadIdx.x, sp + PTF_POFF(i));
+    }
     cp_async_commit();
   }
   C v[E];
@@ -516,6 +590,7 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
     C* __restrict__ S = a.s + boff;
     C* __restrict__ SI = a.si + boff;
     C* __restrict__ AC = a.acc + boff;
+    C* __restrict__ SL = a.slo ? a.slo + boff : nullptr;  // compensated state (FP32)
     const T* __restrict__ Lt = a.Ltab + toff;
     const T* __restrict__ cf = a.coef + 6 * toff;
 #pragma unroll
@@ -526,15 +601,25 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
       if (MODE == COL_PROLOGUE || MODE == COL_YINV3) {
         x = S[o];
       } else if (MODE == COL_FWD_STORE) {
-        x = Nh; if (store) S[o] = x;
+        x = Nh;
+        if (store) {
+          S[o] = x;
+          if (SL) SL[o] = C();  // a new state: no low part
+        }
       } else if (MODE == COL_FWD_N) {
         x = Nh; if (store) a.nout[boff + PTF_OFF(RF, i)] = Nh;  // an intermediate: spectral layout
       } else {
         if (PF && i == 0) cp_async_wait_all();
         auto lf = [&]() { return Lval(Lt, o, i); };
-        x = stage_combine<T, MODE, PF>(Nh, o, S, SI, AC, cf, plane, dt, store, lf,
-                                                        (!BATCHED && a.filt) ? a.filt + toff : nullptr,
-                                                        PF ? park[i * nthr + threadIdx.x] : C());
+        if (PS2 && ps) {
+          x = stage_combine<T, MODE, PF, true>(Nh, o, S, SI, AC, cf, plane, dt, store, lf,
+                                               (!BATCHED && a.filt) ? a.filt + toff : nullptr,
+                                               park[i * nthr + threadIdx.x], SL, park2[i * nthr + threadIdx.x]);
+        } else {
+          x = stage_combine<T, MODE, PF>(Nh, o, S, SI, AC, cf, plane, dt, store, lf,
+                                         (!BATCHED && a.filt) ? a.filt + toff : nullptr,
+                                         PF ? park[i * nthr + threadIdx.x] : C(), SL);
+        }
       }
       if (k0thr && i == 0) {
         // the (0,0) mode in FP64: {s, stage input (ETDRK4: d), acc, -} of this solve
@@ -550,7 +635,10 @@ __device__ __forceinline__ void col_body(const ColArgs<T>& a, int tile, int blk,
         const double Nd = k0N;
         const double xd = k0_combine<MODE>(q, kc, dd, Nd);
         x.x = (T)xd; x.y = 0;
-        if (MODE == COL_FWD_STORE || MODE == COL_RK4_4 || MODE == COL_ETD_4) S[o] = x;
+        if (MODE == COL_FWD_STORE || MODE == COL_RK4_4 || MODE == COL_ETD_4) {
+          S[o] = x;
+          if (SL) SL[o] = C();  // the FP64 mode is exact: no low part
+        }
       }
       park[i * nthr + threadIdx.x] = x;
     }
@@ -648,17 +736,14 @@ template <typename T, int NX> __host__ __device__ constexpr size_t row_smem_byte
 // (-1)^K conj(tw[(K j) mod n]) with tw[m] = exp(-2 pi i m / n).
 template <typename C>
 __device__ __forceinline__ C grid_expi(const C* __restrict__ tw, int K, int j, int n) {
-  int m = (int)(((long long)K * j) % n);
-  if (m < 0) m += n;
+  // n is a power of two and |K j| < 2^31: the residue of K j mod n is a mask
+  const int m = (K * j) & (n - 1);
   const C w = __ldg(tw + m);
   C r;
   r.x = w.x; r.y = -w.y;
   if (K & 1) { r.x = -r.x; r.y = -r.y; }
   return r;
 }
-__device__ __forceinline__ void sin_cos(double x, double* s, double* c) { sincos(x, s, c); }
-__device__ __forceinline__ void sin_cos(float x, float* s, float* c) { sincosf(x, s, c); }
-
 // The scaled cellular flow psi = U cos(Kx x + eps sin(omega t)) cos(Ky y) of a
 // slot at one row: u = -d(psi)/dy, v = d(psi)/dx, times fscale.
 template <typename T> struct CellularRow {
@@ -669,9 +754,9 @@ template <typename T, typename C>
 __device__ __forceinline__ CellularRow<T> cellular_row(const SlotParams<T>& sp, const C* tw, int yrow, int n,
                                                         T stage_c, T fscale) {
   CellularRow<T> r;
-  const double te = sp.t + (sp.time_mode ? (double)stage_c * (double)sp.dt : 0.0);
-  const T phi = sp.eps * (T)sin((double)sp.omega * te);
-  sin_cos(phi, &r.sphi, &r.cphi);
+  const int q = stage_c < (T)0.25 ? 0 : stage_c < (T)0.75 ? 1 : 2;  // stage time t + stage_c dt (slot_phases)
+  r.cphi = sp.ph_c[q];
+  r.sphi = sp.ph_s[q];
   const C ey = grid_expi(tw, sp.Ky, yrow, n);
   r.cy = ey.x; r.sy = ey.y;
   const T kx = (T)sp.Kx * sp.dkx, ky = (T)sp.Ky * sp.dky;
@@ -680,17 +765,18 @@ __device__ __forceinline__ CellularRow<T> cellular_row(const SlotParams<T>& sp, 
   r.Kx = sp.Kx;
   return r;
 }
-// The cellular flow at column x of a row pair (rows r0 = cr0, r1 = cr1 of
-// one slot): the x factor is shared by both rows.
+// The cellular flow at column x of a row pair: r describes row 0, (cy1, sy1)
+// is row 1's y factor; the x factor is shared by both rows.
 template <typename T, typename C>
-__device__ __forceinline__ void cellular_uv2(const CellularRow<T>& r0, const CellularRow<T>& r1, const C* tw, int x,
-                                             int n, T* u0, T* v0, T* u1, T* v1) {
-  const C e = grid_expi(tw, r0.Kx, x, n);
-  const T ct = e.x * r0.cphi - e.y * r0.sphi, st = e.y * r0.cphi + e.x * r0.sphi;
-  *u0 = r0.au * ct * r0.sy;
-  *v0 = r0.av * st * r0.cy;
-  *u1 = r1.au * ct * r1.sy;
-  *v1 = r1.av * st * r1.cy;
+__device__ __forceinline__ void cellular_uv2(const CellularRow<T>& r, T cy1, T sy1, const C* tw, int x, int n, T* u0,
+                                             T* v0, T* u1, T* v1) {
+  const C e = grid_expi(tw, r.Kx, x, n);
+  const T ct = e.x * r.cphi - e.y * r.sphi, st = e.y * r.cphi + e.x * r.sphi;
+  const T uc = r.au * ct, vs = r.av * st;
+  *u0 = uc * r.sy;
+  *v0 = vs * r.cy;
+  *u1 = uc * sy1;
+  *v1 = vs * cy1;
 }
 
 // Input of an inverse x transform of two rows at once: Z[k] = H0[k] + i H1[k],
@@ -865,16 +951,17 @@ __device__ __forceinline__ void row_body(const RowArgs<T>& a, int tile, int blk,
     const bool analytic = BATCHED && a.slots[slot].flow_kind == FLOW_CELLULAR;
     if (analytic) {
       const CellularRow<T> cr0 = cellular_row<T, C>(a.slots[slot], a.tw, yy0, NX, a.stage_c, a.fscale);
-      const CellularRow<T> cr1 = cellular_row<T, C>(a.slots[slot], a.tw, yy0 + 1, NX, a.stage_c, a.fscale);
+      const C ey1 = grid_expi(a.tw, a.slots[slot].Ky, yy0 + 1, NX);  // row 1's y factor
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         T u0, v0, u1, v1;
-        cellular_uv2<T, C>(cr0, cr1, a.tw, reg_pos<NX, RIL, E>(t, i), NX, &u0, &v0, &u1, &v1);
+        cellular_uv2<T, C>(cr0, ey1.x, ey1.y, a.tw, reg_pos<NX, RIL, E>(t, i), NX, &u0, &v0, &u1, &v1);
         const C cx = park[i * TPL + t];
         C w;
         w.x = u0 * cx.x + v0 * v[i].x;
         w.y = u1 * cx.y + v1 * v[i].y;
         v[i] = w;
+        if ((i & 3) == 3) asm volatile("" ::: "memory");  // a few elements' loads in flight at a time
       }
     } else {
 #pragma unroll

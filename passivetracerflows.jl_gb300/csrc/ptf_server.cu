@@ -92,7 +92,8 @@ double points(const ptf_solve_desc& d) {
 size_t handle_estimate(const ptf_server* s, const ptf_solve_desc& d) {
   const size_t n = d.n, pitch = ((n / 2 + 1) + 7) / 8 * 8;
   const size_t e = s->cfg.precision == PTF_FP32 ? 8 : 16, r = e / 2;
-  return 7 * n * n * pitch * e + 5 * n * n * n * r + n * n * n * 8;
+  // 7 spectral fields, 8 with an FP32 handle's compensated state
+  return (s->cfg.precision == PTF_FP32 ? 8 : 7) * n * n * pitch * e + 5 * n * n * n * r + n * n * n * 8;
 }
 
 bool try_admit(ptf_server* s, int64_t id, Request& q) {

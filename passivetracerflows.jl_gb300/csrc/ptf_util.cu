@@ -18,30 +18,45 @@ __global__ void real_out_kernel(const T* __restrict__ src, double* __restrict__ 
 // User row r (of rows_per_solve per solve), bin k <-> element spec_map(m, .)
 // of the solve's plane (rows_per_solve * pitch elements).  Bins k >= nkr of
 // the pitch are written as zero.
+// lo non-null: dst and lo receive the value split into its rounding and the
+// remainder (x = hi + lo exactly for FP32 parts of an FP64 value near hi).
 template <typename T>
 __global__ void spec_in_kernel(const double2* __restrict__ src, typename cplx_of<T>::type* __restrict__ dst, int nkr,
-                               long long rows, long long rows_per_solve, SpecMap m) {
+                               long long rows, long long rows_per_solve, SpecMap m,
+                               typename cplx_of<T>::type* __restrict__ lo) {
   const long long n = rows * m.pitch;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const long long rg = i / m.pitch;
     const int k = (int)(i - rg * m.pitch);
     const long long b = rg / rows_per_solve, r = rg - b * rows_per_solve;
-    typename cplx_of<T>::type z;
-    if (k < nkr) { const double2 s = src[rg * nkr + k]; z.x = (T)s.x; z.y = (T)s.y; }
-    else { z.x = 0; z.y = 0; }
-    dst[b * rows_per_solve * m.pitch + spec_map(m, r, k)] = z;
+    typename cplx_of<T>::type z, zl;
+    zl.x = 0; zl.y = 0;
+    if (k < nkr) {
+      const double2 s = src[rg * nkr + k];
+      z.x = (T)s.x; z.y = (T)s.y;
+      zl.x = (T)(s.x - (double)z.x); zl.y = (T)(s.y - (double)z.y);
+    } else {
+      z.x = 0; z.y = 0;
+    }
+    const long long at = b * rows_per_solve * m.pitch + spec_map(m, r, k);
+    dst[at] = z;
+    if (lo) lo[at] = zl;
   }
 }
 template <typename T>
 __global__ void spec_out_kernel(const typename cplx_of<T>::type* __restrict__ src, double2* __restrict__ dst, int nkr,
-                                long long rows, long long rows_per_solve, SpecMap m) {
+                                long long rows, long long rows_per_solve, SpecMap m,
+                                const typename cplx_of<T>::type* __restrict__ lo) {
   const long long n = rows * nkr;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const long long rg = i / nkr;
     const int k = (int)(i - rg * nkr);
     const long long b = rg / rows_per_solve, r = rg - b * rows_per_solve;
-    const typename cplx_of<T>::type z = src[b * rows_per_solve * m.pitch + spec_map(m, r, k)];
-    dst[i] = make_double2((double)z.x, (double)z.y);
+    const long long at = b * rows_per_solve * m.pitch + spec_map(m, r, k);
+    const typename cplx_of<T>::type z = src[at];
+    double2 d = make_double2((double)z.x, (double)z.y);
+    if (lo) { d.x += (double)lo[at].x; d.y += (double)lo[at].y; }
+    dst[i] = d;
   }
 }
 
@@ -61,22 +76,24 @@ template <typename T> cudaError_t launch_real_out(const T* src, double* dst, lon
 }
 template <typename T>
 cudaError_t launch_spec_in(const double2* src, typename cplx_of<T>::type* dst, int nkr, int pitch, long long rows,
-                           cudaStream_t st, const SpecMap* map, long long rows_per_solve) {
+                           cudaStream_t st, const SpecMap* map, long long rows_per_solve,
+                           typename cplx_of<T>::type* lo) {
   SpecMap m;
   if (map) m = *map;
   m.pitch = pitch;
   if (!map || rows_per_solve <= 0) rows_per_solve = rows;
-  spec_in_kernel<T><<<grid_for(rows * pitch), 256, 0, st>>>(src, dst, nkr, rows, rows_per_solve, m);
+  spec_in_kernel<T><<<grid_for(rows * pitch), 256, 0, st>>>(src, dst, nkr, rows, rows_per_solve, m, lo);
   return cudaGetLastError();
 }
 template <typename T>
 cudaError_t launch_spec_out(const typename cplx_of<T>::type* src, double2* dst, int nkr, int pitch, long long rows,
-                            cudaStream_t st, const SpecMap* map, long long rows_per_solve) {
+                            cudaStream_t st, const SpecMap* map, long long rows_per_solve,
+                            const typename cplx_of<T>::type* lo) {
   SpecMap m;
   if (map) m = *map;
   m.pitch = pitch;
   if (!map || rows_per_solve <= 0) rows_per_solve = rows;
-  spec_out_kernel<T><<<grid_for(rows * nkr), 256, 0, st>>>(src, dst, nkr, rows, rows_per_solve, m);
+  spec_out_kernel<T><<<grid_for(rows * nkr), 256, 0, st>>>(src, dst, nkr, rows, rows_per_solve, m, lo);
   return cudaGetLastError();
 }
 
@@ -247,9 +264,13 @@ template cudaError_t launch_real_in<double>(const double*, double*, long long, d
 template cudaError_t launch_real_in<float>(const double*, float*, long long, double, cudaStream_t);
 template cudaError_t launch_real_out<double>(const double*, double*, long long, cudaStream_t);
 template cudaError_t launch_real_out<float>(const float*, double*, long long, cudaStream_t);
-template cudaError_t launch_spec_in<double>(const double2*, double2*, int, int, long long, cudaStream_t, const SpecMap*, long long);
-template cudaError_t launch_spec_in<float>(const double2*, float2*, int, int, long long, cudaStream_t, const SpecMap*, long long);
-template cudaError_t launch_spec_out<double>(const double2*, double2*, int, int, long long, cudaStream_t, const SpecMap*, long long);
-template cudaError_t launch_spec_out<float>(const float2*, double2*, int, int, long long, cudaStream_t, const SpecMap*, long long);
+template cudaError_t launch_spec_in<double>(const double2*, double2*, int, int, long long, cudaStream_t, const SpecMap*,
+                                            long long, double2*);
+template cudaError_t launch_spec_in<float>(const double2*, float2*, int, int, long long, cudaStream_t, const SpecMap*,
+                                           long long, float2*);
+template cudaError_t launch_spec_out<double>(const double2*, double2*, int, int, long long, cudaStream_t, const SpecMap*,
+                                             long long, const double2*);
+template cudaError_t launch_spec_out<float>(const float2*, double2*, int, int, long long, cudaStream_t, const SpecMap*,
+                                            long long, const float2*);
 
 }  // namespace ptf

@@ -80,7 +80,12 @@ def test_1d_calcN_and_sol(gpu, oracle):
 
 
 def test_1d_fp32_k0_mode(gpu, oracle):
-    """FP32 1D with uniform damping (nκh = 0): the mean follows the FP64 oracle."""
+    """FP32 1D with uniform damping (nκh = 0): the mean follows the FP64 oracle.
+
+    The (0,0) state is FP64, but in 1D its right-hand side N(0) = -sum(u c_x)
+    is not zero (u varies along x): it is summed in FP64 from FP32 products,
+    so its error is that of the FP32 c_x -- about 1e-9 of the mean after 300
+    steps here, where an FP32 (0,0) state would drift by ~1e-6."""
     p, r = pair1(gpu, oracle, 256, stepper="RK4", T=np.float32, κh=0.5, nκh=0)
     x = gpu.gridpoints(p.grid)
     c = 1.0 + ic1(x)
@@ -91,8 +96,8 @@ def test_1d_fp32_k0_mode(gpu, oracle):
     gpu.updatevars(p)
     oracle.updatevars(r)
     r0 = r.sol[0].real
-    assert abs(p.sol[0].real - r0) <= 1e-9 * abs(r0)
-    assert abs(p.vars.c.sum() - r0) <= 1e-9 * abs(r0)
+    assert abs(p.sol[0].real - r0) <= 5e-9 * abs(r0)
+    assert abs(p.vars.c.sum() - r0) <= 5e-9 * abs(r0)
     assert oracle.rel_l2(p.vars.c, r.vars.c) <= 1e-5
 
 
