@@ -362,18 +362,21 @@ double pass_bytes(const ptf_handle* h, int kind, int mode) {
     if (mode == ROW_RHS3) return B * 4 * M + 3 * P;
     return B * (M + P);
   }
+  // the compensated state (FP32 2D/3D): the last stage also reads s and its
+  // low part and writes the low part; set_c writes the low part (zero)
+  const double lo = h->slo ? 1.0 : 0.0;
   switch (mode) {
     case COL_PROLOGUE: return B * 3 * M;
-    case COL_FWD_STORE: return B * 4 * M;
+    case COL_FWD_STORE: return B * (4 + lo) * M;
     case COL_FWD_N: return B * 2 * M;
     case COL_YINV3: return B * 5 * M;
     case COL_RK4_1: return B * 6 * M + Tb;
     case COL_RK4_2: case COL_RK4_3: return B * 8 * M + Tb;
-    case COL_RK4_4: return B * 6 * M + Tb;
+    case COL_RK4_4: return B * (6 + 3 * lo) * M + Tb;
     case COL_ETD_1: return B * 6 * M + 4 * Tb;
     case COL_ETD_2: return B * 6 * M + 3 * Tb;
     case COL_ETD_3: return B * 6 * M + 2 * Tb;
-    default: return B * 5 * M + Tb;  // COL_ETD_4
+    default: return B * (5 + 3 * lo) * M + Tb;  // COL_ETD_4
   }
 }
 

@@ -101,7 +101,7 @@ def test_roofline_traffic_comes_from_the_committed_profile():
     col, src = b.profiled_traffic("column_pass", "f32", 1024, 16)
     row, _ = b.profiled_traffic("row_pass", "f32", 1024, 16)
     assert src == "pass2d_fp32_1024x1024_b16_etdrk4.md"
-    assert col == 351896576 and row == 184454208
+    assert col == 399764672 and row == 183517504
     assert b.profiled_traffic("column_pass", "f32", 2048, 16) == (None, None)
     peak, kind = b.load_peaks()
     assert peak > 1000 and kind in ("measured", "fallback")
