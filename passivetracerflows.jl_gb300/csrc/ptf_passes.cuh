@@ -1119,8 +1119,11 @@ __global__ void __launch_bounds__(256) row_rhs_tma_kernel(RowArgs<T> a) {
 
 // FP32 row blocks are held to 128 registers (two 256-thread blocks, or eight
 // of the default 64 threads, per SM); FP64 takes what it needs.
+#ifndef PTF_ROW_MINB_F32
+#define PTF_ROW_MINB_F32 2
+#endif
 template <typename T> struct RowBounds { static constexpr int blocks = 1; };
-template <> struct RowBounds<float> { static constexpr int blocks = 2; };
+template <> struct RowBounds<float> { static constexpr int blocks = PTF_ROW_MINB_F32; };
 template <typename T, int NX, bool PAIRED = false>
 __global__ void __launch_bounds__(256, RowBounds<T>::blocks) row_pass_kernel(RowArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
