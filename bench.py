@@ -1022,6 +1022,8 @@ def run_served_stream(pkg, T, nreq, rate, seed=5150, pool=8, check=8, max_queued
             "p50_latency_s": st["p50_s"], "p99_latency_s": st["p99_s"], "mean_latency_s": st["mean_s"],
             "grid_pt_steps_per_s": st["grid_point_steps"] / wall, "wall_s": wall, "total_grid_pt_steps": work,
             "peak_device_bytes": st["device_bytes"], "input_prep_s": prep, "feeder_holds": holds[0],
+            "server_time": {"admission_s": st["admit_s"], "stepping_s": st["chunk_s"], "chunks": st["chunks"],
+                            "what": "worker wall time admitting requests and stepping chunks (launch to completion)"},
             "mass_drift_max_abs": max(abs(d) for d in drifts), "mass_drift_median_abs": float(np.median(np.abs(drifts))),
             "diverged": {"count": len(diverged), "examples": diverged[:6],
                          "why": "under-resolved: the advective form, like the reference's, is not dealiased; "

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define PTF_ABI_VERSION 3
+#define PTF_ABI_VERSION 4
 
 enum ptf_status {
   PTF_OK = 0,
@@ -306,6 +306,9 @@ typedef struct ptf_server_stats {
   double mass_drift_max_abs;    /* max over completed requests of |sum(c_end) / sum(c0) - 1| */
   int64_t batch_solves;         /* solves holding a slot of the batched form (2D) */
   int64_t handles;              /* single-solve handles alive (3D) */
+  double admit_s;               /* worker time admitting requests (copies in, set_c, plan) */
+  double chunk_s;               /* worker time from launching a chunk of steps to its completion */
+  int64_t chunks;               /* chunks stepped */
 } ptf_server_stats;
 
 typedef struct ptf_server ptf_server;

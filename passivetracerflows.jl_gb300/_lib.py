@@ -65,7 +65,8 @@ class PtfServerStats(ct.Structure):
     _fields_ = [("completed", ct.c_int64), ("failed", ct.c_int64), ("queued", ct.c_int64), ("active", ct.c_int64),
                 ("p50_s", ct.c_double), ("p99_s", ct.c_double), ("mean_s", ct.c_double),
                 ("grid_point_steps", ct.c_double), ("wall_s", ct.c_double), ("device_bytes", ct.c_int64),
-                ("mass_drift_max_abs", ct.c_double), ("batch_solves", ct.c_int64), ("handles", ct.c_int64)]
+                ("mass_drift_max_abs", ct.c_double), ("batch_solves", ct.c_int64), ("handles", ct.c_int64),
+                ("admit_s", ct.c_double), ("chunk_s", ct.c_double), ("chunks", ct.c_int64)]
 
 
 class PtfTuning(ct.Structure):

@@ -78,6 +78,8 @@ struct ptf_server {
   Clock::time_point t_first, t_last;
   int64_t completed = 0, failed = 0;
   double mass_drift_max = 0.0;
+  double admit_s = 0.0, chunk_s = 0.0;  // worker time in admission, and in stepping chunks to their completion
+  int64_t chunks = 0;
   int inject_fail_in = -1;  // host-side fault injection: fail the chunk this many chunks ahead (-1: none)
   std::string error;
 };
@@ -194,10 +196,12 @@ void drop_failed(ptf_server* s, Request& q, const std::string& why) {
 void worker_loop(ptf_server* s) {
   for (;;) {
     std::vector<ptf_handle*> handles;
+    std::vector<int64_t> hsteps;  // each handle's steps this chunk (to its own count)
     int64_t chunk = 0;
     {
       std::unique_lock<std::mutex> lk(s->mu);
       // admission in arrival order, first fit
+      const Clock::time_point ta = Clock::now();
       for (auto it = s->queue.begin(); it != s->queue.end();) {
         Request& q = s->reqs[*it];
         if (try_admit(s, *it, q)) {
@@ -207,20 +211,26 @@ void worker_loop(ptf_server* s) {
           ++it;
         }
       }
+      s->admit_s += std::chrono::duration<double>(Clock::now() - ta).count();
       if (s->active.empty()) {
         if (s->stop && s->queue.empty()) return;
         s->cv.wait_for(lk, std::chrono::milliseconds(2));
         continue;
       }
+      // The batch retires each slot at its own step count on the device
+      // (its clock kernel), so a chunk need not stop at the soonest
+      // finishing request: 2D requests take the full chunk, 3D handles
+      // step exactly to their own counts.
       chunk = s->cfg.chunk_steps > 0 ? s->cfg.chunk_steps : 50;
       for (int64_t id : s->active) {
         const Request& q = s->reqs[id];
-        chunk = std::min<int64_t>(chunk, q.desc.nsteps - q.done_steps);
+        if (q.handle) {
+          handles.push_back(q.handle);
+          hsteps.push_back(std::min<int64_t>(chunk, q.desc.nsteps - q.done_steps));
+        }
       }
-      chunk = std::max<int64_t>(chunk, 1);
-      for (int64_t id : s->active)
-        if (s->reqs[id].handle) handles.push_back(s->reqs[id].handle);
     }
+    const Clock::time_point tc = Clock::now();
     bool injected = false;
     {
       std::lock_guard<std::mutex> lk(s->mu);
@@ -234,10 +244,10 @@ void worker_loop(ptf_server* s) {
     else if (rc) why = std::string("batched step: ") + ptf_batch_last_error(s->batch);
     // 3D handles: enqueue every handle's chunk (their streams run beside the
     // batch's), then wait for each
-    for (ptf_handle* h : handles) {
+    for (size_t k = 0; k < handles.size(); ++k) {
       if (rc) break;
-      rc = ptf_step(h, chunk);
-      if (rc) why = std::string("3D step: ") + ptf_last_error(h);
+      rc = ptf_step(handles[k], hsteps[k]);
+      if (rc) why = std::string("3D step: ") + ptf_last_error(handles[k]);
     }
     for (ptf_handle* h : handles) {
       if (rc) break;
@@ -250,6 +260,8 @@ void worker_loop(ptf_server* s) {
     }
     {
       std::lock_guard<std::mutex> lk(s->mu);
+      s->chunk_s += std::chrono::duration<double>(Clock::now() - tc).count();
+      s->chunks++;
       if (rc) s->error = why;
       std::vector<int64_t> still;
       for (int64_t id : s->active) {
@@ -426,6 +438,9 @@ int ptf_server_get_stats(ptf_server* s, ptf_server_stats* out) {
   }
   out->grid_point_steps = s->grid_point_steps;
   out->mass_drift_max_abs = s->mass_drift_max;
+  out->admit_s = s->admit_s;
+  out->chunk_s = s->chunk_s;
+  out->chunks = s->chunks;
   int64_t live = 0;
   for (const auto& kv : s->reqs) if (kv.second.handle) ++live;
   out->handles = live;

@@ -53,7 +53,7 @@ def test_config_defaults_match_reference(pkg):
     assert (c.nx, c.ny) == (128, 128)
     assert abs(c.Lx - 6.283185307179586) < 1e-15 and c.kappa == 0.1 and c.eta == 0.1 and c.dt == 0.01
     assert c.stepper == 0 and c.batch == 1
-    assert lib.ptf_abi_version() == 3
+    assert lib.ptf_abi_version() == 4
 
 
 @pytest.mark.parametrize("field,value,msg", [
