@@ -553,24 +553,23 @@ def run_workloads(args, pkg, torch):
     """The secondary configurations (rank 0): each entry carries its own
     timing, accuracy and the seconds it took; a failure is reported in place."""
     workloads = {}
-    if True:
-        for key, fn in (("2d_cellular_4096", lambda: run_config2_4096(pkg, torch, args.config_steps_2d)),
-                        ("3d_abc_256", lambda: run_abc3d_256(pkg, torch, args.config_steps_3d)),
-                        ("ensemble_256_solves", lambda: run_ensemble_256(pkg, torch, args.ensemble_steps)),
-                        ("ensemble_256_solves_clock_t",
-                         lambda: run_ensemble_256(pkg, torch, args.ensemble_steps, time_mode="clock",
-                                                  fp64_check=False)),
-                        ("served_fp32", lambda: run_served_stream(pkg, np.float32, args.serve_requests, args.serve_rate)),
-                        ("served_fp64", lambda: run_served_stream(pkg, np.float64, args.serve_requests_fp64,
-                                                            args.serve_rate / 8, check=0))):
-            if args.only and key not in args.only.split(","):
-                continue
-            try:
-                t_w = time.perf_counter()
-                workloads[key] = fn()
-                workloads[key]["bench_seconds"] = time.perf_counter() - t_w
-            except Exception as e:  # report the failure in the line rather than losing the main result
-                workloads[key] = {"error": f"{type(e).__name__}: {e}"}
+    for key, fn in (("2d_cellular_4096", lambda: run_config2_4096(pkg, torch, args.config_steps_2d)),
+                    ("3d_abc_256", lambda: run_abc3d_256(pkg, torch, args.config_steps_3d)),
+                    ("ensemble_256_solves", lambda: run_ensemble_256(pkg, torch, args.ensemble_steps)),
+                    ("ensemble_256_solves_clock_t",
+                     lambda: run_ensemble_256(pkg, torch, args.ensemble_steps, time_mode="clock",
+                                              fp64_check=False)),
+                    ("served_fp32", lambda: run_served_stream(pkg, np.float32, args.serve_requests, args.serve_rate)),
+                    ("served_fp64", lambda: run_served_stream(pkg, np.float64, args.serve_requests_fp64,
+                                                        args.serve_rate / 8, check=0))):
+        if args.only and key not in args.only.split(","):
+            continue
+        try:
+            t_w = time.perf_counter()
+            workloads[key] = fn()
+            workloads[key]["bench_seconds"] = time.perf_counter() - t_w
+        except Exception as e:  # report the failure in the line rather than losing the main result
+            workloads[key] = {"error": f"{type(e).__name__}: {e}"}
     return workloads
 
 
