@@ -412,6 +412,64 @@ __device__ __forceinline__ void fft_line(C* v, int t, C* line, const C* __restri
   StagesFrom<N, DIR, E, 1, NST>::run(v, t, line, tw);
 }
 
+// ---------------------------------------------------------------------------
+// Mirror-paired last stage.  When the last stage of a forward transform has
+// a radix R < E (a remainder stage), each thread holds E/R >= 2 of its
+// butterflies, and they can be chosen so that a thread holds both X[p] and
+// X[N - p] for every output p it holds: butterfly j's outputs are
+// j + r B (B = N/R) and N - (j + r B) = (B - j) + (R - 1 - r) B, so j and
+// B - j are paired (0 with B/2, each of which mirrors itself).  Thread t
+// holds j = t + q TPL for q < m (m = E/(2R)) in slots q, and their partners
+// in slots q + m.  The row pass then separates the two rows' spectra of a
+// packed transform in registers instead of through shared memory.
+template <int N, int E> struct MirrorLast {
+  static constexpr int R = Sched<N, E>::REM;
+  static constexpr bool ok = R > 1 && E / R >= 2;
+  static constexpr int B = N / (R > 1 ? R : 1), TPL = N / E, M = E / (2 * (R > 1 ? R : 1));
+};
+template <int N, int E> __device__ __forceinline__ int mirror_butterfly(int t, int q) {
+  constexpr int B = MirrorLast<N, E>::B, TPL = MirrorLast<N, E>::TPL, M = MirrorLast<N, E>::M;
+  if (q < M) return t + q * TPL;
+  const int jl = t + (q - M) * TPL;
+  return jl == 0 ? B / 2 : B - jl;
+}
+
+// Forward transform (DIR = -1) of one line whose last (remainder) stage runs
+// on the mirror-paired butterflies: on exit v[q R + r] holds X at position
+// mirror_butterfly(t, q) + r B.  Every thread of the block must call this.
+template <int N, int E = FFT_E, typename C>
+__device__ __forceinline__ void fft_line_mirror_last(C* v, int t, C* line, const C* __restrict__ tw) {
+  constexpr int DIR = -1;
+  constexpr int NST = Sched<N, E>::NSTAGES;
+  constexpr int R = MirrorLast<N, E>::R, B = MirrorLast<N, E>::B;
+  static_assert(MirrorLast<N, E>::ok && NST >= 2, "mirror-paired last stage needs a remainder stage");
+  static_assert(stage_radix<N, DIR, E>(NST - 1) == R, "the forward transform's remainder stage is its last");
+  constexpr int R0 = stage_radix<N, DIR, E>(0);
+  stage_compute<N, R0, 1, DIR, E>(v, t, tw);
+  StagesFrom<N, DIR, E, 1, NST - 1>::run(v, t, line, tw);
+  constexpr int RP = stage_radix<N, DIR, E>(NST - 2);
+  constexpr int NSP = StageNS<N, DIR, E, NST - 2>::value;
+  constexpr int NS = StageNS<N, DIR, E, NST - 1>::value;
+  static_assert(NS == B, "the last stage's sub-transform size");
+  __syncthreads();
+  stage_store<N, RP, NSP, E>(v, t, line);
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < E / R; ++q) {
+    const int j = mirror_butterfly<N, E>(t, q);
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[q * R + r] = line[smem_pad(j + r * B)];
+    // twiddles w^(r j) (k = j mod NS = j), then the radix-R DFT; outputs at j + r B
+    if constexpr ((R == 8) && sizeof(C) == 8) {
+      TwiddledDFT<R, DIR, C>::run(v + q * R, tw, j);
+    } else {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[q * R + r] = cmul_tw<DIR>(v[q * R + r], ldtw(tw, r * j));
+      DFT<R, DIR, C>::run(v + q * R);
+    }
+  }
+}
+
 template <int N, int DIR, int E = FFT_E> struct FirstRadix {
   static constexpr int value = (Sched<N, E>::REM > 1 && DIR > 0) ? Sched<N, E>::REM : E;
 };

@@ -982,22 +982,46 @@ __device__ __forceinline__ void row_body(const RowArgs<T>& a, int tile, int blk,
       }
     }
   }
-  // forward x-FFT of n_y0 + i n_y1
-  fft_line<NX, -1, E>(v, t, line, a.tw);
-  __syncthreads();
-#pragma unroll
-  for (int i = 0; i < E; ++i) line[smem_pad(reg_pos<NX, RFL, E>(t, i))] = v[i];
-  __syncthreads();
+  // forward x-FFT of n_y0 + i n_y1, separated into the two rows' half
+  // spectra: row y0 W[k] + conj(W[n-k]), row y1 -i (W[k] - conj(W[n-k]))
   const T sc = a.scale;
-  if (valid) {
-    for (int k = t; k <= NX / 2; k += TPL) {
-      const C wk = line[smem_pad(k)];
-      const C wn = line[smem_pad((NX - k) & (NX - 1))];
-      C o0, o1;
-      // row y0: W[k] + conj(W[n-k]) ; row y1: -i (W[k] - conj(W[n-k]))
-      o0.x = (wk.x + wn.x) * sc; o0.y = (wk.y - wn.y) * sc;
-      o1.x = (wk.y + wn.y) * sc; o1.y = (wn.x - wk.x) * sc;
-      st_pair<PAIRED>(a.out + r0, a.out + r1, k << yl, o0, o1);
+  auto emit = [&](int k, C wk, C wn) {
+    C o0, o1;
+    o0.x = (wk.x + wn.x) * sc; o0.y = (wk.y - wn.y) * sc;
+    o1.x = (wk.y + wn.y) * sc; o1.y = (wn.x - wk.x) * sc;
+    st_pair<PAIRED>(a.out + r0, a.out + r1, k << yl, o0, o1);
+  };
+  if constexpr (MirrorLast<NX, E>::ok) {
+    // last stage on mirror-paired butterflies: W[k] and W[n-k] are in this
+    // thread's registers (MirrorLast), so no shared-memory round trip
+    fft_line_mirror_last<NX, E>(v, t, line, a.tw);
+    constexpr int R = MirrorLast<NX, E>::R, B = MirrorLast<NX, E>::B, M = MirrorLast<NX, E>::M;
+    if (valid) {
+#pragma unroll
+      for (int q = 0; q < M; ++q) {
+        const int j = t + q * TPL;  // slot q; slot q + M holds B - j (B/2 when j = 0)
+#pragma unroll
+        for (int r = 0; r < R / 2; ++r) {
+          if (q == 0 && t == 0) {
+            // butterfly 0 (outputs r B, mirrored within itself) and butterfly B/2
+            emit(r * B, v[r], v[(R - r) % R]);
+            emit(B / 2 + r * B, v[M * R + r], v[M * R + R - 1 - r]);
+          } else {
+            emit(j + r * B, v[q * R + r], v[(q + M) * R + R - 1 - r]);
+            emit(B - j + r * B, v[(q + M) * R + r], v[q * R + R - 1 - r]);
+          }
+        }
+      }
+      if (t == 0) emit(NX / 2, v[R / 2], v[R / 2]);  // k = n/2 = (R/2) B: butterfly 0, output R/2
+    }
+  } else {
+    fft_line<NX, -1, E>(v, t, line, a.tw);
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < E; ++i) line[smem_pad(reg_pos<NX, RFL, E>(t, i))] = v[i];
+    __syncthreads();
+    if (valid) {
+      for (int k = t; k <= NX / 2; k += TPL) emit(k, line[smem_pad(k)], line[smem_pad((NX - k) & (NX - 1))]);
     }
   }
 }
