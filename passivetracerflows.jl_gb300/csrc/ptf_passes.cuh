@@ -366,7 +366,15 @@ __device__ __forceinline__ C stage_combine(const C Nh, int o, C* __restrict__ S,
       C lo = SLO[o];
       add_compensated(hi.x, lo.x, d.x);
       add_compensated(hi.y, lo.y, d.y);
-      if (filt) { const T f = filt[o]; hi.x *= f; hi.y *= f; lo.x *= f; lo.y *= f; }
+      if (filt) {
+        // scale both parts, then renormalise (fast two-sum) so the pair stays canonical
+        const T f = filt[o];
+        C h, l;
+        h.x = hi.x * f; h.y = hi.y * f;
+        l.x = lo.x * f; l.y = lo.y * f;
+        hi.x = h.x + l.x; hi.y = h.y + l.y;
+        lo.x = l.x - (hi.x - h.x); lo.y = l.y - (hi.y - h.y);
+      }
       if (store) SLO[o] = lo;
     } else {
       hi = d;

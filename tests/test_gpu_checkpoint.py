@@ -40,6 +40,7 @@ def _ic(gpu, p, batch):
     (2, 64, "ETDRK4", np.float64, 1, False),
     (3, 32, "ETDRK4", np.float32, 1, True),
     (1, 256, "FilteredRK4", np.float64, 2, True),
+    (2, 128, "FilteredETDRK4", np.float32, 2, True),  # the compensated pair through the filter
 ])
 def test_resume_is_bit_identical(gpu, tmp_path, dim, n, stepper, T, batch, steady):
     a = _make(gpu, dim, n, stepper, T, batch, steady)
