@@ -121,6 +121,20 @@ def profiled_traffic(kernel, precision, n, batch):
     return None, None
 
 
+def profiled_fp64_pipe(kernel, n):
+    """FP64-pipe activity (% of peak over the launch, ncu
+    sm__pipe_fp64_cycles_active) of an FP64 pass, as recorded in a summary
+    under profiles/ by a line ``fp64-pipe-active: <kernel> f64 n=<n> pct=<P>``."""
+    import re
+    pat = re.compile(r"fp64-pipe-active:\s+(\S+)\s+f64\s+n=(\d+)\s+pct=([0-9.]+)")
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        for line in f.read_text().splitlines():
+            m = pat.search(line)
+            if m and m.group(1) == kernel and int(m.group(2)) == n:
+                return float(m.group(3)), f.name
+    return None, None
+
+
 def fft_flops_2d_rhs(nx, ny):
     """FP64 operation count of one 2D right-hand side by the usual FFT
     convention (5 N log2 N flops per complex transform of length N): the
@@ -465,6 +479,13 @@ def run_ours(args):
               "flops_per_step": fp64_flops_step,
               "flop_model": "5 N log2 N per complex FFT; 3 column + 1.5 row transforms per line per RHS; 4 RHS/step",
               "hbm_GBps_algorithmic": bytes64_step / (ms64 / K64 / 1e3) / 1e9}
+    # the FP64 pipe's measured activity in the same passes (the flop model
+    # above counts a radix-2 FFT's operations; the radix-16 transforms issue
+    # fewer, so the pipe is busier than `frac` suggests)
+    pipe = {k: profiled_fp64_pipe(k, n) for k in ("column_pass", "row_pass")}
+    if all(v[0] is not None for v in pipe.values()):
+        roof64["fp64_pipe_active_pct_ncu"] = {k: v[0] for k, v in pipe.items()}
+        roof64["fp64_pipe_source"] = pipe["column_pass"][1]
     # ---------------- accuracy vs the FP64 oracle ----------------
     # The bench's own problems, restarted from the initial condition and
     # stepped over the configured 1000 steps (t = 0.5 at dt = 5e-4); solve 0

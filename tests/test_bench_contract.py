@@ -105,3 +105,14 @@ def test_roofline_traffic_comes_from_the_committed_profile():
     assert b.profiled_traffic("column_pass", "f32", 2048, 16) == (None, None)
     peak, kind = b.load_peaks()
     assert peak > 1000 and kind in ("measured", "fallback")
+
+
+def test_fp64_pipe_activity_comes_from_the_committed_profile():
+    """`fp64_plain.roofline` carries the FP64-pipe activity ncu measured in
+    the same passes, read from profiles/."""
+    b = _bench()
+    col, src = b.profiled_fp64_pipe("column_pass", 1024)
+    row, _ = b.profiled_fp64_pipe("row_pass", 1024)
+    assert src == "pass2d_fp64_1024x1024_b1_etdrk4.md"
+    assert col == 69.0 and row == 68.4
+    assert b.profiled_fp64_pipe("column_pass", 4096) == (None, None)
