@@ -10,6 +10,8 @@ import os
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libptf.so"
+# PTF_ABI_VERSION of include/ptf.h that the structs and signatures below mirror
+ABI_VERSION = 4
 
 PTF_OK, PTF_ERR_ARG, PTF_ERR_CUDA, PTF_ERR_STATE, PTF_ERR_UNSUPPORTED, PTF_ERR_MEMORY = 0, 1, 2, 3, 4, 5
 PTF_RK4, PTF_ETDRK4, PTF_FILTERED_RK4, PTF_FILTERED_ETDRK4 = 0, 1, 2, 3
@@ -168,6 +170,12 @@ def load(path: os.PathLike | None = None):
     if not p.exists():
         raise RuntimeError(f"{p} is missing: build it first (passivetracerflows.jl_gb300/build.py)")
     lib = ct.CDLL(str(p))
+    lib.ptf_abi_version.restype = ct.c_int32
+    lib.ptf_abi_version.argtypes = []
+    got = lib.ptf_abi_version()
+    if got != ABI_VERSION:
+        raise RuntimeError(f"{p} has ABI version {got}, this binding needs {ABI_VERSION}: rebuild it "
+                           "(passivetracerflows.jl_gb300/build.py)")
     for name, (res, args) in SIGNATURES.items():
         f = getattr(lib, name)
         f.restype = res

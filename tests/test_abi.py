@@ -37,6 +37,15 @@ def test_python_binding_covers_header(pkg):
     assert not missing, missing
 
 
+def test_binding_abi_version_matches_header_and_library(pkg):
+    """The Python binding refuses a library of another ABI version; the
+    version it expects is the header's, and the built library reports it."""
+    from ptf_gb300 import _lib
+    m = re.search(r"#define\s+PTF_ABI_VERSION\s+(\d+)", (ROOT / "include" / "ptf.h").read_text())
+    assert m and int(m.group(1)) == _lib.ABI_VERSION
+    assert _lib.load().ptf_abi_version() == _lib.ABI_VERSION
+
+
 def _cfg(pkg, **kw):
     from ptf_gb300 import _lib as L
     lib = L.load()
